@@ -1,0 +1,146 @@
+"""Pin the CPU oracle against the reference's own fixtures and functions.
+
+``pbmc1k_knn.npz`` is the reference's test data (scarf/tests/datasets,
+checked by scarf/tests/test_datastore.py:66-79); ``ref_functions.npz`` holds
+outputs of the reference's own functions executed from its source by
+``tests/golden/make_golden.py``.
+"""
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle
+
+
+@pytest.fixture(scope="module")
+def kat(golden_dir):
+    return np.load(os.path.join(golden_dir, "pbmc1k_knn.npz"))
+
+
+@pytest.fixture(scope="module")
+def ref(golden_dir):
+    return np.load(os.path.join(golden_dir, "ref_functions.npz"))
+
+
+def test_smoothing_known_answer(kat):
+    # test_graph_weights (test_datastore.py:76-79), made two-sided
+    edges, w = oracle.smoothen_dists(kat["indices"], kat["distances"], 1.0, 1.5, 1000)
+    assert np.abs(w - kat["weights"]).max() < 1e-5
+    n, k = kat["indices"].shape
+    assert np.array_equal(edges[:, 0], np.repeat(np.arange(n), k))
+    assert np.array_equal(edges[:, 1], kat["indices"].ravel())
+    # the first weight of every row is exactly 1.0 (rho is the first distance)
+    assert np.all(w.reshape(n, k)[:, 0] == 1.0)
+
+
+def test_smoothing_column0_is_skipped(kat):
+    # including column 0 in the sigma sum breaks the known answer
+    d = kat["distances"].astype(np.float32)
+    sig, rho = oracle.smooth_knn_dist(d, 11, local_connectivity=1.0, bandwidth=1.5)
+    d2 = np.concatenate([np.zeros((d.shape[0], 1), np.float32), d], axis=1)
+    sig2, _ = oracle.smooth_knn_dist(d2, 11, local_connectivity=1.0, bandwidth=1.5)
+    assert not np.allclose(sig, sig2)
+
+
+def test_smoothen_dists_chunk_loop(ref):
+    edges, w = oracle.smoothen_dists(ref["smooth_idx"], ref["smooth_dist"], 1.0, 1.5,
+                                     int(ref["smooth_chunk"]))
+    assert np.array_equal(edges, ref["smooth_edges"])
+    assert np.array_equal(w, ref["smooth_w"])
+    # the chunk-local self check of compute_membership_strengths fires in later chunks
+    assert (ref["smooth_w"] == ref["smooth_w"].min()).sum() >= 1
+
+
+def test_clean_array(ref):
+    assert np.array_equal(oracle.clean_array(ref["clean_in"]), ref["clean_out0"])
+    assert np.array_equal(oracle.clean_array(ref["clean_in"], 1), ref["clean_out1"])
+
+
+def test_norm_lib_size_log(ref):
+    c = ref["norm_counts"]
+    m = sp.csr_matrix(c)
+    x, _ = oracle.normed_csr(m.indptr, m.indices, m.data.astype(np.int32), c.shape[1],
+                             np.arange(c.shape[1]))
+    assert np.array_equal(x, ref["norm_log"])
+
+
+def test_fix_knn_query(ref):
+    fi, fd, nm = oracle.fix_knn_query(ref["fix_ind"], ref["fix_dist"], ref["fix_ref"])
+    assert np.array_equal(fi, ref["fix_out_i"])
+    assert np.array_equal(fd, ref["fix_out_d"])
+    assert nm == int(ref["fix_nmis"])
+
+
+def test_self_query_knn(ref):
+    pts = ref["sqk_points"]
+    k = int(ref["sqk_k"])
+    i, d, rec = oracle.self_query_knn(pts, k, int(ref["sqk_chunk"]))
+    assert np.array_equal(i, ref["sqk_indices"])
+    assert np.array_equal(d, ref["sqk_distances"])
+    assert rec == pytest.approx(float(ref["sqk_recall"]))
+
+
+def _csr(ref, p):
+    return ref[p + "_indptr"], ref[p + "_indices"], ref[p + "_data"]
+
+
+def test_symmetrize_and_fuzzy_union(ref):
+    n = int(ref["union_n"])
+    edges = np.stack([ref["union_rows"], ref["union_cols"]], 1)
+    k = len(ref["union_rows"]) // n
+    g = oracle.store_to_sparse(edges, ref["union_w"], n, k)
+    s = oracle.symmetrize(g)
+    s.sort_indices()
+    for got, want in zip((s.indptr, s.indices, s.data), _csr(ref, "sym")):
+        assert np.array_equal(got, want)
+    for mix, p in ((1.0, "fss"), (0.7, "fss07")):
+        u = oracle.fuzzy_simplicial_set(g, mix).tocsr()
+        u.sort_indices()
+        for got, want in zip((u.indptr, u.indices, u.data), _csr(ref, p)):
+            assert np.array_equal(got, want)
+
+
+def test_incremental_pca_block_order(ref):
+    x = ref["pca_x"]
+    mu, sd = ref["pca_mu"], ref["pca_sigma"]
+    z = (x - mu) / sd
+    b = int(ref["pca_batch"])
+    blocks = [z[s:s + b] for s in range(0, z.shape[0], b)]
+    load, pca = oracle.fit_pca_reference_order(blocks, int(ref["pca_dims"]), ref["pca_use"])
+    want = ref["pca_loadings"]
+    assert load.shape == want.shape
+    assert np.abs(load - want).max() < 1e-8
+    assert np.abs(pca.explained_variance_ratio_ - ref["pca_evr"]).max() < 1e-10
+
+
+def test_incremental_pca_vs_sklearn():
+    skd = pytest.importorskip("sklearn.decomposition")
+    rng = np.random.default_rng(3)
+    z = rng.normal(size=(500, 30)) @ rng.normal(size=(30, 30))
+    ours = oracle.IncrementalPCARestated(8)
+    theirs = skd.IncrementalPCA(n_components=8)
+    for s in range(0, 500, 120):
+        ours.partial_fit(z[s:s + 120])
+        theirs.partial_fit(z[s:s + 120])
+    assert np.abs(ours.components_ - theirs.components_).max() < 1e-8
+
+
+def test_exact_pca_spans_ipca_subspace():
+    rng = np.random.default_rng(4)
+    base = rng.normal(size=(2000, 5)) * np.array([9, 7, 5, 4, 3.0])
+    z = np.hstack([base, 0.1 * rng.normal(size=(2000, 15))]) @ np.linalg.qr(rng.normal(size=(20, 20)))[0]
+    comps, _ = oracle.pca_exact(z, 6)
+    blocks = [z[s:s + 300] for s in range(0, 2000, 300)]
+    load, _ = oracle.fit_pca_reference_order(blocks, 5)
+    ang = oracle.subspace_angles(comps[:, :5], load)
+    assert ang.max() < 1e-3
+
+
+def test_exact_knn_tie_order():
+    pts = np.array([[0.0], [1.0], [1.0], [2.0], [5.0]])
+    i, d = oracle.exact_knn(pts, pts, 4)
+    assert i[0].tolist() == [0, 1, 2, 3]
+    assert i[1].tolist() == [1, 2, 0, 3]
+    assert i[2].tolist() == [1, 2, 0, 3]
