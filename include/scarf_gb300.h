@@ -1,0 +1,164 @@
+/*
+ * scarf_gb300 -- C ABI of the GB300 (sm_103a) graph-construction path of scarf.
+ *
+ * Every entry point takes caller-owned DEVICE pointers (plain pointers and
+ * sizes, no C++ or torch types), an explicit cudaStream_t passed as void*, and
+ * returns an int status (SG_OK = 0, negative on error; the message is in
+ * sg_last_error(), which is per host thread). Calls are asynchronous on the
+ * given stream unless stated otherwise; completion means the caller has
+ * synchronised that stream. The library never frees caller memory. Scratch
+ * memory belongs to the handle: it grows on demand up to the handle's HBM
+ * budget and is reused by later calls, so calls made with one handle must be
+ * issued on one stream (or be ordered by the caller). One handle per host
+ * thread.
+ *
+ * Reference paths are relative to the scarf project root (v0.32.3).
+ */
+#ifndef SCARF_GB300_H
+#define SCARF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sg_handle sg_handle;
+
+enum {
+  SG_OK = 0,
+  SG_ERR_ARG = -1,         /* bad shape, size, pointer or flag */
+  SG_ERR_OOM = -2,         /* device allocation failed */
+  SG_ERR_CUDA = -3,        /* a CUDA runtime / library call failed */
+  SG_ERR_TIMEOUT = -4,     /* a bounded device wait ran out */
+  SG_ERR_BUDGET = -5,      /* scratch would exceed the handle's HBM budget */
+  SG_ERR_UNSUPPORTED = -6  /* valid request this build does not implement */
+};
+
+/* element types */
+enum { SG_F32 = 0, SG_BF16 = 1, SG_F64 = 2 };
+/* numeric forms */
+enum { SG_PLAIN = 0, SG_PRECISION = 1 };
+/* sg_normalize_csr flags */
+#define SG_NORM_LOG1P 1u          /* log_transform=True   (scarf/assay.py:54-64) */
+#define SG_NORM_RENORM_SUBSET 2u  /* renormalize_subset=True (scarf/assay.py:818-823) */
+/* sg_fuzzy_union flags */
+#define SG_UNION_UPPER_ONLY 1u    /* load_graph(upper_only=True): triu (graph_datastore.py:1071-1072) */
+
+int sg_version(void);
+const char* sg_last_error(void);
+
+/* Create a handle on `device` whose scratch may grow to `hbm_budget_bytes`
+ * (0 = no limit). No reference counterpart: scarf holds no device state. */
+int sg_create(int device, size_t hbm_budget_bytes, sg_handle** out);
+int sg_destroy(sg_handle* h);
+/* Bytes of scratch the handle holds now. */
+size_t sg_workspace_bytes(const sg_handle* h);
+
+/* a1+a3 -- library-size normalisation of CSR counts with the feature gather,
+ * fused with the column sums of the written values.
+ * Replaces RNAassay.normed (scarf/assay.py:780-828) with norm_lib_size /
+ * norm_lib_size_log (scarf/assay.py:41-64) and the two statistics passes of
+ * make_graph (scarf/datastore/graph_datastore.py:767-796).
+ *   indptr[n_rows+1]: row r's entries are indices/data[indptr[r]-indptr[0] ..
+ *   indptr[r+1]-indptr[0]); col_map[n_genes]: output column of a gene or -1.
+ *   s_r = integer sum of the mapped counts (0 -> 1) when SG_NORM_RENORM_SUBSET,
+ *   else n_counts[r]. out[r*ld_out + j] = log1p(size_factor*c/s_r) (or without
+ *   log1p), written as SG_F32 or SG_BF16. Columns with missing_mask[j] != 0
+ *   take fill_value instead (mapping_utils.py:208 fills 1.0); missing_mask may
+ *   be NULL. libsize_out[n_rows] (int64, may be NULL) receives s_r for the
+ *   renormalised form. colsum/colsumsq (n_cols doubles, may be NULL) are
+ *   ACCUMULATED with the sums of the written values, in a fixed order. */
+int sg_normalize_csr(sg_handle* h, const int64_t* indptr, const int32_t* indices,
+                     const int32_t* data, int64_t n_rows, const int32_t* col_map,
+                     int64_t n_genes, int32_t n_cols, const uint8_t* missing_mask,
+                     float fill_value, const double* n_counts, double size_factor,
+                     uint32_t flags, void* out, int64_t ld_out, int32_t out_dtype,
+                     int64_t* libsize_out, double* colsum, double* colsumsq, void* stream);
+
+/* a3 -- mu = sum/n, sigma = sqrt(sumsq/n - mu^2) (population std), then
+ * clean_array: NaN/inf -> 0 and sigma == 0 -> 1 (scarf/utils.py:143-153,
+ * graph_datastore.py:767-796). f32 copies (may be NULL) feed the kernels. */
+int sg_zstats(sg_handle* h, const double* colsum, const double* colsumsq, int64_t n_rows,
+              int32_t n_cols, double* mu, double* sigma, float* mu32, float* sigma32,
+              void* stream);
+
+/* a4 -- scatter of the z-scaled rows, z = (x - mu)/sigma, over rows with
+ * row_mask[r] != 0 (row_mask may be NULL = all): cov (n_cols^2 doubles,
+ * symmetric, row-major) and zsum (n_cols doubles) are ACCUMULATED.
+ * SG_PLAIN: FP32 SIMT products; SG_PRECISION: 3xBF16 split products on the
+ * tcgen05 tensor cores with FP32 accumulation. Partials are reduced in FP64.
+ * Replaces the IncrementalPCA fit of AnnStream._fit_pca (scarf/ann.py:207-256). */
+int sg_covariance(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld,
+                  const float* mu32, const float* sigma32, const uint8_t* row_mask,
+                  int32_t precision, double* cov, double* zsum, void* stream);
+
+/* a4 -- principal axes of the centred scatter cov - zsum zsum^T / n_used by an
+ * FP64 eigendecomposition on the device. comps[n_cols*n_comp] (row-major,
+ * column c = c-th largest) with the largest-magnitude entry of each component
+ * positive (scikit-learn svd_flip(u_based_decision=False)); evals[n_comp]
+ * descending; evr[n_comp] = eval / trace (explained_variance_ratio_);
+ * loadings32[n_cols*ld_l] = the first n_load components as float32 (the
+ * reference's loadings = components_[:-1].T, ann.py:256). Synchronises the
+ * stream. Any output pointer except comps may be NULL. */
+int sg_pca_basis(sg_handle* h, const double* cov, const double* zsum, int64_t n_used,
+                 int32_t n_cols, int32_t n_comp, double* comps, double* evals, double* evr,
+                 int32_t n_load, float* loadings32, int32_t ld_l, void* stream);
+
+/* a5 -- the reducer ((x - mu)/sigma) . L (scarf/ann.py:129-138, :191-192):
+ * scores[r*ld_s + c], c < d (columns d..ld_s-1 are written 0). bf16_out (may be
+ * NULL) receives a BF16 copy with row stride ld_b (zero padded). */
+int sg_project(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld,
+               const float* mu32, const float* sigma32, const float* loadings32, int32_t d,
+               int32_t ld_l, float* scores, int32_t ld_s, void* bf16_out, int32_t ld_b,
+               void* stream);
+
+/* a6/a7/a10 -- exact squared-L2 kNN of queries[nq x d] (row stride ld) against
+ * refs[nr x d], replacing the hnswlib index (scarf/ann.py:14-28, :290-326) and
+ * AnnStream.transform_ann (scarf/ann.py:194-205).
+ * self_offset >= 0: query q is reference row self_offset+q; k+1 neighbours are
+ *   found and self is removed with fix_knn_query's rule (scarf/ann.py:31-52):
+ *   column 0 if it is self, else the first self position, else the last
+ *   column; *n_missed (device int64, ACCUMULATED) counts rows whose first hit
+ *   was not self, i.e. self_query_knn's recall (scarf/knn_utils.py:23-76).
+ * self_offset < 0: plain query of k neighbours (run_mapping,
+ *   scarf/datastore/mapping_datastore.py:198-208); n_missed may be NULL.
+ * precision SG_PLAIN: FP32 candidate distances; SG_PRECISION: BF16 tcgen05
+ * distance GEMM. Both keep k(+1)+margin candidates per query and re-rank them
+ * with exact FP32 sum((q-r)^2), ties by index. idx_out[nq*k] int64,
+ * dist_out[nq*k] float32 (hnswlib 'l2' returns squared distances). */
+int sg_knn(sg_handle* h, const float* queries, int64_t nq, const float* refs, int64_t nr,
+           int32_t d, int32_t ld, int32_t k, int64_t self_offset, int32_t margin,
+           int32_t precision, int64_t* idx_out, float* dist_out, int64_t* n_missed,
+           void* stream);
+
+/* a8 -- smoothen_dists (scarf/knn_utils.py:89-159) over umap-learn's
+ * smooth_knn_dist and compute_membership_strengths, chunk by chunk of
+ * chunk_rows rows: rho/sigma per row (sigma sum from column 1), weights in
+ * float32, weight 0 where the neighbour index equals the chunk-local row, then
+ * zero weights replaced by global_min = min(1, smallest non-zero weight of each
+ * chunk holding a zero). edges_out[n*k*2] int64 pairs (row, col) in row-major
+ * order (the (n*k, 2) u8 dataset), w_out[n*k] float64. */
+int sg_smooth(sg_handle* h, const int64_t* knn_idx, const float* knn_dist, int64_t n,
+              int32_t k, double local_connectivity, double bandwidth, int64_t chunk_rows,
+              int64_t* edges_out, double* w_out, void* stream);
+
+/* a9 -- fuzzy union of the graph G given as COO (edges[nnz*2] int64 pairs,
+ * w[nnz] float64, k edges per row in row-major order; use_k < k keeps the first
+ * use_k of each row as _store_to_sparse does, graph_datastore.py:474-511;
+ * duplicates are summed): U = mix*(G + G^T - G o G^T) + (1-mix)*(G o G^T)
+ * with zeros removed (umap.py:118-123; mix = 1 is load_graph's symmetrize,
+ * graph_datastore.py:1052-1055). FP64 with the reference's operation order,
+ * so values are bit-identical to scipy's. Output CSR with sorted column
+ * indices: indptr_out[n+1] (int64; indptr_out[n] is the nnz), indices_out and
+ * data_out with room for `capacity` entries (2*nnz always suffices). */
+int sg_fuzzy_union(sg_handle* h, const int64_t* edges, const double* w, int64_t nnz, int64_t n,
+                   int32_t k, int32_t use_k, double mix, uint32_t flags, int64_t* indptr_out,
+                   int32_t* indices_out, double* data_out, int64_t capacity, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCARF_GB300_H */

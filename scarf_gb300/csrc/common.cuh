@@ -1,0 +1,93 @@
+// Shared definitions of the scarf_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <cstdint>
+#include <cstddef>
+
+#include "../../include/scarf_gb300.h"
+
+struct sg_handle {
+  int device = 0;
+  int sm_count = 0;
+  size_t smem_optin = 0;
+  size_t budget = 0;         // 0 = unlimited
+  void* ws = nullptr;        // scratch arena, grown on demand
+  size_t ws_bytes = 0;
+  void* solver = nullptr;    // cusolverDnHandle_t, created on first use
+  void* solver_work = nullptr;
+  size_t solver_work_bytes = 0;
+};
+
+namespace sg {
+
+int fail(int status, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+void clear_error();
+
+// Scratch of at least `bytes`, 256-byte aligned; grows the arena (after a
+// device synchronisation) when needed. nullptr on failure with the error set.
+void* ws_get(sg_handle* h, size_t bytes, int* status);
+
+// Carves consecutive 256-byte-aligned pieces out of one scratch block.
+struct Carver {
+  char* base;
+  size_t off = 0;
+  explicit Carver(void* b) : base(static_cast<char*>(b)) {}
+  template <class T>
+  T* take(size_t count) {
+    T* p = reinterpret_cast<T*>(base + off);
+    off += (count * sizeof(T) + 255) & ~size_t(255);
+    return p;
+  }
+  static size_t need(size_t bytes) { return (bytes + 255) & ~size_t(255); }
+};
+
+inline int ceil_div_i(int64_t a, int64_t b) { return int((a + b - 1) / b); }
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace sg
+
+#define SG_ARG(cond, ...)                                   \
+  do {                                                      \
+    if (!(cond)) return sg::fail(SG_ERR_ARG, __VA_ARGS__);  \
+  } while (0)
+
+#define SG_CUDA(call)                                                   \
+  do {                                                                  \
+    cudaError_t e_ = (call);                                            \
+    if (e_ != cudaSuccess) return sg::cuda_fail(e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define SG_LAUNCH_CHECK() SG_CUDA(cudaGetLastError())
+
+#define SG_HANDLE_CHECK(h)                                            \
+  do {                                                                \
+    if (!(h)) return sg::fail(SG_ERR_ARG, "null sg_handle");          \
+    sg::clear_error();                                                \
+    SG_CUDA(cudaSetDevice((h)->device));                              \
+  } while (0)
+
+// ---- device helpers --------------------------------------------------------
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}

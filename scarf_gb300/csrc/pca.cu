@@ -1,0 +1,438 @@
+// a4 + a5: scatter (covariance) of the z-scaled rows, FP64 eigendecomposition
+// of it on the device (cuSOLVER syevdx, top n_comp pairs), the svd_flip sign
+// convention, and the reducer projection ((x - mu)/sigma) . L.
+//
+// Plain covariance: FP32 SIMT, 128x128 output tiles of the upper triangle,
+// 8x8 register micro-tiles, rows split into K-chunks whose float32 partials are
+// reduced in FP64 in a fixed order. The z-transform (and the PCA row mask) is
+// applied while staging each 16-row slab into shared memory.
+#include "common.cuh"
+
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <vector>
+
+int sg_covariance_tc(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld,
+                     const float* mu32, const float* sigma32, const uint8_t* row_mask, double* cov,
+                     double* zsum, cudaStream_t st);  // cov_tc.cu
+
+namespace {
+
+constexpr int CT = 128;  // covariance output tile
+constexpr int CBK = 16;  // rows per shared-memory slab
+
+__device__ __forceinline__ float zval(float x, float m, float s) { return __fdiv_rn(x - m, s); }
+
+// t-th tile (row-major) of the upper triangle of a T x T tile grid
+__device__ __forceinline__ int2 upper_tile(int t, int T) {
+  for (int i = 0; i < T; ++i) {
+    const int cnt = T - i;
+    if (t < cnt) return make_int2(i, i + t);
+    t -= cnt;
+  }
+  return make_int2(T - 1, T - 1);
+}
+
+// grid: (n_upper_tiles, n_splits). Tile t enumerates (ti, tj) with tj >= ti.
+__global__ void __launch_bounds__(256, 2)
+cov_simt_kernel(const float* __restrict__ x, int64_t n_rows, int n_cols, int64_t ld,
+                const float* __restrict__ mu, const float* __restrict__ sg, const uint8_t* __restrict__ mask,
+                int T, int64_t rows_per_split, float* __restrict__ part,
+                int n_pad, float* __restrict__ zpart) {
+  __shared__ __align__(16) float As[2][CBK][CT];
+  __shared__ __align__(16) float Bs[2][CBK][CT];
+  const int tid = threadIdx.x;
+  const int2 t = upper_tile(blockIdx.x, T);
+  const int i0 = t.x * CT, j0 = t.y * CT;
+  const bool diag = t.x == t.y;
+  const int64_t r_begin = int64_t(blockIdx.y) * rows_per_split;
+  const int64_t r_end = min(n_rows, r_begin + rows_per_split);
+  const int tx = tid & 15, ty = tid >> 4;
+  // loader mapping: slab row lk = tid / 16, 8 columns from (tid % 16) * 8
+  const int lk = tid >> 4, lc = (tid & 15) * 8;
+
+  float acc[8][8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a)
+#pragma unroll
+    for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+  float zs[8];
+#pragma unroll
+  for (int a = 0; a < 8; ++a) zs[a] = 0.f;
+
+  float ra[8], rb[8];
+  auto load = [&](int64_t r0) {
+    const int64_t r = r0 + lk;
+    const bool ok = r < r_end && (mask == nullptr || mask[r] != 0);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int ca = i0 + lc + q, cb = j0 + lc + q;
+      ra[q] = (ok && ca < n_cols) ? zval(x[r * ld + ca], mu[ca], sg[ca]) : 0.f;
+      rb[q] = (ok && cb < n_cols) ? zval(x[r * ld + cb], mu[cb], sg[cb]) : 0.f;
+    }
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      As[buf][lk][lc + q] = ra[q];
+      Bs[buf][lk][lc + q] = rb[q];
+    }
+    if (diag) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) zs[q] += ra[q];
+    }
+  };
+
+  int buf = 0;
+  if (r_begin < r_end) {
+    load(r_begin);
+    store(0);
+  }
+  __syncthreads();
+  for (int64_t r0 = r_begin; r0 < r_end; r0 += CBK) {
+    const bool more = r0 + CBK < r_end;
+    if (more) load(r0 + CBK);
+#pragma unroll
+    for (int kk = 0; kk < CBK; ++kk) {
+      float a[8], b[8];
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][kk][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][kk][64 + ty * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][kk][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][kk][64 + tx * 4]);
+      a[0] = a0.x; a[1] = a0.y; a[2] = a0.z; a[3] = a0.w;
+      a[4] = a1.x; a[5] = a1.y; a[6] = a1.z; a[7] = a1.w;
+      b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w;
+      b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
+#pragma unroll
+      for (int p = 0; p < 8; ++p)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[p][q] = fmaf(a[p], b[q], acc[p][q]);
+    }
+    if (more) store(buf ^ 1);
+    __syncthreads();
+    buf ^= 1;
+  }
+  // write the float32 partial tile
+  float* P = part + int64_t(blockIdx.y) * n_pad * n_pad;
+#pragma unroll
+  for (int p = 0; p < 8; ++p) {
+    const int gi = i0 + (p < 4 ? ty * 4 + p : 64 + ty * 4 + p - 4);
+    float4 lo = make_float4(acc[p][0], acc[p][1], acc[p][2], acc[p][3]);
+    float4 hi = make_float4(acc[p][4], acc[p][5], acc[p][6], acc[p][7]);
+    *reinterpret_cast<float4*>(&P[int64_t(gi) * n_pad + j0 + tx * 4]) = lo;
+    *reinterpret_cast<float4*>(&P[int64_t(gi) * n_pad + j0 + 64 + tx * 4]) = hi;
+  }
+  if (diag) {
+    // column sums of z over this split: 16 loader rows share each column
+    __syncthreads();
+    float* red = &As[0][0][0];  // 16 x 128 floats
+#pragma unroll
+    for (int q = 0; q < 8; ++q) red[lk * CT + lc + q] = zs[q];
+    __syncthreads();
+    if (tid < CT) {
+      float s = 0.f;
+      for (int r = 0; r < CBK; ++r) s += red[r * CT + tid];
+      zpart[int64_t(blockIdx.y) * n_pad + i0 + tid] = s;
+    }
+  }
+}
+
+// FP64 sum over splits (fixed order) of the upper-triangle tiles; the result
+// is added to cov[i][j] and mirrored to cov[j][i].
+__global__ void cov_reduce_kernel(const float* __restrict__ part, int nsplit, int n_pad, int n_cols, int T,
+                                  double* __restrict__ cov) {
+  const int2 t = upper_tile(blockIdx.x, T);
+  for (int e = threadIdx.x; e < CT * CT; e += blockDim.x) {
+    const int i = t.x * CT + e / CT, j = t.y * CT + e % CT;
+    if (i >= n_cols || j >= n_cols || j < i) continue;
+    double s = 0.0;
+    for (int p = 0; p < nsplit; ++p) s += double(part[int64_t(p) * n_pad * n_pad + int64_t(i) * n_pad + j]);
+    cov[int64_t(i) * n_cols + j] += s;
+    if (i != j) cov[int64_t(j) * n_cols + i] += s;
+  }
+}
+
+__global__ void zsum_reduce_kernel(const float* __restrict__ zpart, int nsplit, int n_pad, int n_cols,
+                                   double* __restrict__ zsum) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_cols) return;
+  double s = 0.0;
+  for (int p = 0; p < nsplit; ++p) s += double(zpart[int64_t(p) * n_pad + j]);
+  zsum[j] += s;
+}
+
+// centred scatter A = cov - zsum zsum^T / n, and its trace
+__global__ void center_kernel(const double* __restrict__ cov, const double* __restrict__ zsum, double inv_n,
+                              int n, double* __restrict__ A) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= int64_t(n) * n) return;
+  const int i = int(e / n), j = int(e % n);
+  const double c = zsum ? zsum[i] * zsum[j] * inv_n : 0.0;
+  A[e] = cov[e] - c;
+}
+
+__global__ void trace_kernel(const double* __restrict__ A, int n, double* __restrict__ out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += A[int64_t(i) * n + i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// One CTA per output component c (descending eigenvalue order).
+__global__ void basis_kernel(const double* __restrict__ V, const double* __restrict__ W, int n, int m,
+                             const double* __restrict__ trace, double* __restrict__ comps,
+                             double* __restrict__ evals, double* __restrict__ evr, int n_load,
+                             float* __restrict__ L32, int ld_l) {
+  __shared__ double bv[256];
+  __shared__ int bi[256];
+  const int c = blockIdx.x;
+  const int src = m - 1 - c;  // syevdx returns ascending order
+  const double* v = V + int64_t(src) * n;  // column-major eigenvectors
+  double best = -1.0;
+  int besti = 0x7fffffff;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double a = fabs(v[i]);
+    if (a > best) { best = a; besti = i; }
+  }
+  bv[threadIdx.x] = best;
+  bi[threadIdx.x] = besti;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      const double a = bv[threadIdx.x + o];
+      const int ai = bi[threadIdx.x + o];
+      if (a > bv[threadIdx.x] || (a == bv[threadIdx.x] && ai < bi[threadIdx.x])) {
+        bv[threadIdx.x] = a;
+        bi[threadIdx.x] = ai;
+      }
+    }
+    __syncthreads();
+  }
+  const double sgn = v[bi[0]] < 0.0 ? -1.0 : 1.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double val = sgn * v[i];
+    comps[int64_t(i) * m + c] = val;
+    if (L32 && c < n_load) L32[int64_t(i) * ld_l + c] = float(val);
+  }
+  if (L32 && c < n_load) {
+    for (int i = threadIdx.x; i < n && c == 0; i += blockDim.x)
+      for (int cc = n_load; cc < ld_l; ++cc) L32[int64_t(i) * ld_l + cc] = 0.f;
+  }
+  if (threadIdx.x == 0) {
+    if (evals) evals[c] = W[src];
+    if (evr) evr[c] = W[src] / *trace;
+  }
+}
+
+// ---- projection -----------------------------------------------------------
+constexpr int PR = 128;  // rows per CTA
+constexpr int PC = 64;   // output columns per CTA
+constexpr int PK = 32;   // features per slab
+
+__global__ void __launch_bounds__(256)
+project_kernel(const float* __restrict__ x, int64_t n_rows, int n_cols, int64_t ld, const float* __restrict__ mu,
+               const float* __restrict__ sg, const float* __restrict__ L, int d, int ld_l,
+               float* __restrict__ scores, int ld_s, __nv_bfloat16* __restrict__ sb, int ld_b) {
+  __shared__ __align__(16) float As[PK][PR + 4];
+  __shared__ __align__(16) float Bs[PK][PC];
+  const int tid = threadIdx.x;
+  const int64_t r0 = int64_t(blockIdx.x) * PR;
+  const int c0 = blockIdx.y * PC;
+  const int tx = tid & 15, ty = tid >> 4;
+  float acc[8][4];
+#pragma unroll
+  for (int p = 0; p < 8; ++p)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[p][q] = 0.f;
+  const int lr = tid >> 1, lj = (tid & 1) * 16;
+  for (int j0 = 0; j0 < n_cols; j0 += PK) {
+    const int64_t r = r0 + lr;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int j = j0 + lj + q;
+      As[lj + q][lr] = (r < n_rows && j < n_cols) ? zval(x[r * ld + j], mu[j], sg[j]) : 0.f;
+    }
+    for (int e = tid; e < PK * PC; e += 256) {
+      const int jj = e / PC, cc = e % PC;
+      const int j = j0 + jj, c = c0 + cc;
+      Bs[jj][cc] = (j < n_cols && c < d) ? L[int64_t(j) * ld_l + c] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < PK; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[kk][64 + ty * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[4] = {b0.x, b0.y, b0.z, b0.w};
+#pragma unroll
+      for (int p = 0; p < 8; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(a[p], b[q], acc[p][q]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < 8; ++p) {
+    const int64_t r = r0 + (p < 4 ? ty * 4 + p : 64 + ty * 4 + p - 4);
+    if (r >= n_rows) continue;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = c0 + tx * 4 + q;
+      const float v = c < d ? acc[p][q] : 0.f;
+      if (c < ld_s) scores[r * ld_s + c] = v;
+      if (sb && c < ld_b) sb[r * ld_b + c] = __float2bfloat16_rn(v);
+    }
+  }
+}
+
+__global__ void pad_cols_kernel(float* __restrict__ s, int64_t n_rows, int from, int ld,
+                                __nv_bfloat16* __restrict__ sb, int from_b, int ld_b) {
+  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= n_rows) return;
+  for (int c = from; c < ld; ++c) s[r * ld + c] = 0.f;
+  if (sb)
+    for (int c = from_b; c < ld_b; ++c) sb[r * ld_b + c] = __float2bfloat16_rn(0.f);
+}
+
+
+}  // namespace
+
+void sg_solver_destroy(sg_handle* h) {
+  if (h->solver) cusolverDnDestroy(static_cast<cusolverDnHandle_t>(h->solver));
+  if (h->solver_work) cudaFree(h->solver_work);
+  h->solver = nullptr;
+  h->solver_work = nullptr;
+}
+
+extern "C" int sg_covariance(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld,
+                             const float* mu32, const float* sigma32, const uint8_t* row_mask,
+                             int32_t precision, double* cov, double* zsum, void* stream) {
+  SG_HANDLE_CHECK(h);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  SG_ARG(x && mu32 && sigma32 && cov && zsum, "sg_covariance: null pointer argument");
+  SG_ARG(n_rows >= 0 && n_cols > 0 && ld >= n_cols, "sg_covariance: bad sizes");
+  SG_ARG(precision == SG_PLAIN || precision == SG_PRECISION, "sg_covariance: unknown precision %d", precision);
+  if (n_rows == 0) return SG_OK;
+  if (precision == SG_PRECISION) return sg_covariance_tc(h, x, n_rows, n_cols, ld, mu32, sigma32, row_mask, cov, zsum, st);
+
+  const int T = sg::ceil_div_i(n_cols, CT);
+  const int n_pad = T * CT;
+  const int ntile = T * (T + 1) / 2;
+  int64_t rows_per_split = 8192;
+  const int64_t want_ctas = int64_t(h->sm_count) * 4;
+  while (rows_per_split > 512 && ntile * sg::ceil_div(n_rows, rows_per_split) < want_ctas) rows_per_split /= 2;
+  rows_per_split = ((rows_per_split + CBK - 1) / CBK) * CBK;
+  const int nsplit = int(sg::ceil_div(n_rows, rows_per_split));
+
+  const size_t part_bytes = size_t(nsplit) * n_pad * n_pad * sizeof(float);
+  const size_t need = sg::Carver::need(part_bytes) + sg::Carver::need(size_t(nsplit) * n_pad * sizeof(float));
+  int status;
+  void* w = sg::ws_get(h, need, &status);
+  if (!w) return status;
+  sg::Carver cv(w);
+  float* part = cv.take<float>(size_t(nsplit) * n_pad * n_pad);
+  float* zpart = cv.take<float>(size_t(nsplit) * n_pad);
+  dim3 grid(ntile, nsplit);
+  cov_simt_kernel<<<grid, 256, 0, st>>>(x, n_rows, n_cols, ld, mu32, sigma32, row_mask, T, rows_per_split, part,
+                                        n_pad, zpart);
+  SG_LAUNCH_CHECK();
+  cov_reduce_kernel<<<ntile, 256, 0, st>>>(part, nsplit, n_pad, n_cols, T, cov);
+  SG_LAUNCH_CHECK();
+  zsum_reduce_kernel<<<sg::ceil_div_i(n_cols, 256), 256, 0, st>>>(zpart, nsplit, n_pad, n_cols, zsum);
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
+
+extern "C" int sg_pca_basis(sg_handle* h, const double* cov, const double* zsum, int64_t n_used,
+                            int32_t n_cols, int32_t n_comp, double* comps, double* evals, double* evr,
+                            int32_t n_load, float* loadings32, int32_t ld_l, void* stream) {
+  SG_HANDLE_CHECK(h);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  SG_ARG(cov && comps && n_cols > 0 && n_used > 0, "sg_pca_basis: bad arguments");
+  SG_ARG(n_comp >= 1 && n_comp <= n_cols, "sg_pca_basis: n_comp=%d outside [1, %d]", n_comp, n_cols);
+  SG_ARG(!loadings32 || (n_load >= 0 && n_load <= n_comp && ld_l >= n_load), "sg_pca_basis: bad loadings shape");
+  const int n = n_cols;
+  if (!h->solver) {
+    cusolverDnHandle_t s;
+    if (cusolverDnCreate(&s) != CUSOLVER_STATUS_SUCCESS) return sg::fail(SG_ERR_CUDA, "cusolverDnCreate failed");
+    h->solver = s;
+  }
+  cusolverDnHandle_t sol = static_cast<cusolverDnHandle_t>(h->solver);
+  if (cusolverDnSetStream(sol, st) != CUSOLVER_STATUS_SUCCESS) return sg::fail(SG_ERR_CUDA, "cusolverDnSetStream failed");
+
+  const size_t abytes = sizeof(double) * size_t(n) * n;
+  int status;
+  void* w = sg::ws_get(h, sg::Carver::need(abytes) + sg::Carver::need(sizeof(double) * n) + 1024, &status);
+  if (!w) return status;
+  sg::Carver cv(w);
+  double* A = cv.take<double>(size_t(n) * n);
+  double* W = cv.take<double>(n);
+  double* tr = cv.take<double>(1);
+  int* info = cv.take<int>(1);
+  const int64_t ne = int64_t(n) * n;
+  center_kernel<<<sg::ceil_div_i(ne, 256), 256, 0, st>>>(cov, zsum, 1.0 / double(n_used), n, A);
+  SG_LAUNCH_CHECK();
+  trace_kernel<<<1, 256, 0, st>>>(A, n, tr);
+  SG_LAUNCH_CHECK();
+  const int il = n - n_comp + 1, iu = n;
+  int meig = 0, lwork = 0;
+  if (cusolverDnDsyevdx_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER, n, A, n,
+                                   0.0, 0.0, il, iu, &meig, W, &lwork) != CUSOLVER_STATUS_SUCCESS)
+    return sg::fail(SG_ERR_CUDA, "cusolverDnDsyevdx_bufferSize failed");
+  const size_t wbytes = sizeof(double) * size_t(lwork);
+  if (h->solver_work_bytes < wbytes) {
+    if (h->solver_work) cudaFree(h->solver_work);
+    h->solver_work = nullptr;
+    h->solver_work_bytes = 0;
+    if (h->budget && wbytes + h->ws_bytes > h->budget)
+      return sg::fail(SG_ERR_BUDGET, "eigensolver workspace of %zu bytes exceeds the HBM budget", wbytes);
+    SG_CUDA(cudaMalloc(&h->solver_work, wbytes));
+    h->solver_work_bytes = wbytes;
+  }
+  cusolverStatus_t cs = cusolverDnDsyevdx(sol, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER, n,
+                                          A, n, 0.0, 0.0, il, iu, &meig, W, static_cast<double*>(h->solver_work), lwork,
+                                          info);
+  if (cs != CUSOLVER_STATUS_SUCCESS) return sg::fail(SG_ERR_CUDA, "cusolverDnDsyevdx failed (status %d)", int(cs));
+  int hinfo = 0;
+  SG_CUDA(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(cudaStreamSynchronize(st));
+  if (hinfo != 0) return sg::fail(SG_ERR_CUDA, "cusolverDnDsyevdx: info=%d", hinfo);
+  if (meig != n_comp) return sg::fail(SG_ERR_CUDA, "cusolverDnDsyevdx returned %d of %d eigenpairs", meig, n_comp);
+  basis_kernel<<<n_comp, 256, 0, st>>>(A, W, n, n_comp, tr, comps, evals, evr, n_load, loadings32, ld_l);
+  SG_LAUNCH_CHECK();
+  SG_CUDA(cudaStreamSynchronize(st));
+  return SG_OK;
+}
+
+extern "C" int sg_project(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld,
+                          const float* mu32, const float* sigma32, const float* loadings32, int32_t d,
+                          int32_t ld_l, float* scores, int32_t ld_s, void* bf16_out, int32_t ld_b,
+                          void* stream) {
+  SG_HANDLE_CHECK(h);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  SG_ARG(x && mu32 && sigma32 && loadings32 && scores, "sg_project: null pointer argument");
+  SG_ARG(n_rows >= 0 && n_cols > 0 && ld >= n_cols && d > 0 && ld_l >= d && ld_s >= d, "sg_project: bad sizes");
+  SG_ARG(!bf16_out || ld_b >= d, "sg_project: ld_b < d");
+  if (n_rows == 0) return SG_OK;
+  const int ccols = std::max<int>(ld_s, bf16_out ? ld_b : 0);
+  dim3 grid(sg::ceil_div_i(n_rows, PR), sg::ceil_div_i(std::min<int>(ccols, sg::ceil_div_i(d, PC) * PC), PC));
+  project_kernel<<<grid, 256, 0, st>>>(x, n_rows, n_cols, ld, mu32, sigma32, loadings32, d, ld_l, scores, ld_s,
+                                       static_cast<__nv_bfloat16*>(bf16_out), ld_b);
+  SG_LAUNCH_CHECK();
+  const int covered = int(grid.y) * PC;
+  if (covered < ld_s || (bf16_out && covered < ld_b)) {
+    pad_cols_kernel<<<sg::ceil_div_i(n_rows, 256), 256, 0, st>>>(scores, n_rows, std::min(covered, ld_s), ld_s,
+                                                                 static_cast<__nv_bfloat16*>(bf16_out),
+                                                                 std::min(covered, bf16_out ? ld_b : 0), ld_b);
+    SG_LAUNCH_CHECK();
+  }
+  return SG_OK;
+}

@@ -1,0 +1,255 @@
+"""torch-tensor wrappers over the C ABI (one call per hot-path kernel group).
+
+Inputs and outputs are CUDA tensors; every call is issued on torch's current
+stream of the tensors' device. These wrappers check shapes, dtypes and
+contiguity and raise on any failure of the library (there is no CPU path).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from typing import Optional, Tuple
+
+import torch
+
+from . import _lib as L
+
+_tls = threading.local()
+_budget = {"bytes": 0}
+
+PRECISIONS = {"plain": L.SG_PLAIN, "precision": L.SG_PRECISION}
+
+
+def set_hbm_budget(nbytes: int) -> None:
+    """Scratch budget of handles created after this call (0 = no limit)."""
+    _budget["bytes"] = int(nbytes)
+
+
+class Handle:
+    """Owns one ``sg_handle`` (scratch arena + solver state) on one device."""
+
+    def __init__(self, device: int, budget: int = 0):
+        lib = L.load()
+        self.device = device
+        self.ptr = C.c_void_p()
+        L.check(lib.sg_create(device, budget, C.byref(self.ptr)))
+
+    def workspace_bytes(self) -> int:
+        return int(L.load().sg_workspace_bytes(self.ptr))
+
+    def close(self):
+        if self.ptr:
+            L.load().sg_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def handle(device: Optional[int] = None) -> Handle:
+    if not torch.cuda.is_available():
+        raise RuntimeError("scarf_gb300 needs a CUDA GPU (GB300); none is visible")
+    dev = torch.cuda.current_device() if device is None else int(device)
+    hs = getattr(_tls, "handles", None)
+    if hs is None:
+        hs = _tls.handles = {}
+    h = hs.get(dev)
+    if h is None:
+        h = hs[dev] = Handle(dev, _budget["bytes"])
+    return h
+
+
+def reset_handles() -> None:
+    hs = getattr(_tls, "handles", {})
+    for h in hs.values():
+        h.close()
+    _tls.handles = {}
+
+
+def _p(t: Optional[torch.Tensor]):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream(device) -> C.c_void_p:
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _need(t: torch.Tensor, name: str, dtype=None, ndim=None, contiguous=True):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if dtype is not None and t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    if ndim is not None and t.dim() != ndim:
+        raise ValueError(f"{name} must be {ndim}-D, got shape {tuple(t.shape)}")
+    if contiguous and not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+
+
+def round_up(x: int, m: int) -> int:
+    return (x + m - 1) // m * m
+
+
+# --------------------------------------------------------------------------
+def normalize_csr(indptr, indices, data, col_map, n_cols: int, *, size_factor: float = 1000.0,
+                  log_transform: bool = True, renormalize_subset: bool = True, n_counts=None,
+                  missing_mask=None, fill_value: float = 1.0, out=None, out_dtype=torch.float32,
+                  colsum=None, colsumsq=None, libsize=None) -> torch.Tensor:
+    """a1: dense normalised rows (n_rows x ld) from CSR counts; see sg_normalize_csr."""
+    _need(indptr, "indptr", torch.int64, 1)
+    _need(indices, "indices", torch.int32, 1)
+    _need(data, "data", torch.int32, 1)
+    _need(col_map, "col_map", torch.int32, 1)
+    n_rows = indptr.numel() - 1
+    dev = indptr.device
+    if out is None:
+        ld = round_up(n_cols, 4 if out_dtype == torch.float32 else 8)
+        out = torch.empty((n_rows, ld), dtype=out_dtype, device=dev)
+    _need(out, "out", out_dtype, 2, contiguous=False)
+    if out.stride(1) != 1:
+        raise ValueError("out must have unit column stride")
+    flags = (L.SG_NORM_LOG1P if log_transform else 0) | (L.SG_NORM_RENORM_SUBSET if renormalize_subset else 0)
+    if n_counts is not None:
+        _need(n_counts, "n_counts", torch.float64, 1)
+    if missing_mask is not None:
+        _need(missing_mask, "missing_mask", torch.uint8, 1)
+    if colsum is not None:
+        _need(colsum, "colsum", torch.float64, 1)
+        _need(colsumsq, "colsumsq", torch.float64, 1)
+    if libsize is not None:
+        _need(libsize, "libsize", torch.int64, 1)
+    h = handle(dev.index)
+    lib = L.load()
+    L.check(lib.sg_normalize_csr(
+        h.ptr, _p(indptr), _p(indices), _p(data), n_rows, _p(col_map), col_map.numel(), n_cols,
+        _p(missing_mask), float(fill_value), _p(n_counts), float(size_factor), flags, _p(out),
+        out.stride(0), L.SG_F32 if out_dtype == torch.float32 else L.SG_BF16, _p(libsize), _p(colsum),
+        _p(colsumsq), _stream(dev)))
+    return out
+
+
+def zstats(colsum: torch.Tensor, colsumsq: torch.Tensor, n_rows: int):
+    """a3: (mu, sigma) float64 with clean_array semantics, and float32 copies."""
+    _need(colsum, "colsum", torch.float64, 1)
+    _need(colsumsq, "colsumsq", torch.float64, 1)
+    h = colsum.numel()
+    dev = colsum.device
+    mu = torch.empty(h, dtype=torch.float64, device=dev)
+    sigma = torch.empty_like(mu)
+    mu32 = torch.empty(h, dtype=torch.float32, device=dev)
+    sigma32 = torch.empty_like(mu32)
+    L.check(L.load().sg_zstats(handle(dev.index).ptr, _p(colsum), _p(colsumsq), int(n_rows), h, _p(mu),
+                               _p(sigma), _p(mu32), _p(sigma32), _stream(dev)))
+    return mu, sigma, mu32, sigma32
+
+
+def covariance(x: torch.Tensor, mu32: torch.Tensor, sigma32: torch.Tensor, n_cols: Optional[int] = None,
+               row_mask: Optional[torch.Tensor] = None, precision: str = "plain", cov=None, zsum=None):
+    """a4: accumulate the scatter of the z-scaled rows (cov, zsum) in float64."""
+    _need(x, "x", torch.float32, 2, contiguous=False)
+    if x.stride(1) != 1:
+        raise ValueError("x must have unit column stride")
+    h = int(n_cols if n_cols is not None else mu32.numel())
+    dev = x.device
+    if cov is None:
+        cov = torch.zeros((h, h), dtype=torch.float64, device=dev)
+    if zsum is None:
+        zsum = torch.zeros(h, dtype=torch.float64, device=dev)
+    if row_mask is not None:
+        _need(row_mask, "row_mask", torch.uint8, 1)
+    L.check(L.load().sg_covariance(handle(dev.index).ptr, _p(x), x.shape[0], h, x.stride(0), _p(mu32),
+                                   _p(sigma32), _p(row_mask), PRECISIONS[precision], _p(cov), _p(zsum),
+                                   _stream(dev)))
+    return cov, zsum
+
+
+def pca_basis(cov: torch.Tensor, zsum: Optional[torch.Tensor], n_used: int, n_comp: int,
+              n_load: Optional[int] = None, ld_l: Optional[int] = None):
+    """a4: top ``n_comp`` principal axes (FP64 eigh on the device, svd_flip signs).
+
+    Returns ``(comps h x n_comp f64, evals, evr, loadings32 h x ld_l)`` where
+    loadings32 holds the first ``n_load`` (default n_comp - 1) components."""
+    _need(cov, "cov", torch.float64, 2)
+    h = cov.shape[0]
+    dev = cov.device
+    n_load = n_comp - 1 if n_load is None else n_load
+    ld_l = max(1, n_load) if ld_l is None else ld_l
+    comps = torch.empty((h, n_comp), dtype=torch.float64, device=dev)
+    evals = torch.empty(n_comp, dtype=torch.float64, device=dev)
+    evr = torch.empty(n_comp, dtype=torch.float64, device=dev)
+    l32 = torch.empty((h, ld_l), dtype=torch.float32, device=dev)
+    L.check(L.load().sg_pca_basis(handle(dev.index).ptr, _p(cov), _p(zsum), int(n_used), h, n_comp, _p(comps),
+                                  _p(evals), _p(evr), n_load, _p(l32), ld_l, _stream(dev)))
+    return comps, evals, evr, l32
+
+
+def project(x: torch.Tensor, mu32, sigma32, loadings32: torch.Tensor, d: int, n_cols: Optional[int] = None,
+            ld_s: Optional[int] = None, bf16_ld: Optional[int] = None):
+    """a5: scores = ((x - mu)/sigma) . L as float32 (n x ld_s), optionally a BF16 copy."""
+    _need(x, "x", torch.float32, 2, contiguous=False)
+    _need(loadings32, "loadings32", torch.float32, 2)
+    h = int(n_cols if n_cols is not None else mu32.numel())
+    dev = x.device
+    ld_s = round_up(d, 4) if ld_s is None else ld_s
+    scores = torch.empty((x.shape[0], ld_s), dtype=torch.float32, device=dev)
+    sb = None
+    if bf16_ld:
+        sb = torch.empty((x.shape[0], bf16_ld), dtype=torch.bfloat16, device=dev)
+    L.check(L.load().sg_project(handle(dev.index).ptr, _p(x), x.shape[0], h, x.stride(0), _p(mu32), _p(sigma32),
+                                _p(loadings32), d, loadings32.stride(0), _p(scores), ld_s, _p(sb),
+                                bf16_ld or 0, _stream(dev)))
+    return (scores, sb) if bf16_ld else scores
+
+
+def knn(queries: torch.Tensor, refs: torch.Tensor, d: int, k: int, self_offset: int = -1, margin: int = 0,
+        precision: str = "plain", n_missed: Optional[torch.Tensor] = None):
+    """a6/a7/a10: exact squared-L2 kNN (see sg_knn). Returns ``(idx int64, dist f32, n_missed)``."""
+    _need(queries, "queries", torch.float32, 2)
+    _need(refs, "refs", torch.float32, 2)
+    if queries.shape[1] != refs.shape[1]:
+        raise ValueError("queries and refs must share the row stride")
+    dev = queries.device
+    nq = queries.shape[0]
+    idx = torch.empty((nq, k), dtype=torch.int64, device=dev)
+    dist = torch.empty((nq, k), dtype=torch.float32, device=dev)
+    if n_missed is None:
+        n_missed = torch.zeros(1, dtype=torch.int64, device=dev)
+    L.check(L.load().sg_knn(handle(dev.index).ptr, _p(queries), nq, _p(refs), refs.shape[0], d,
+                            queries.shape[1], k, int(self_offset), int(margin), PRECISIONS[precision], _p(idx),
+                            _p(dist), _p(n_missed), _stream(dev)))
+    return idx, dist, n_missed
+
+
+def smooth(idx: torch.Tensor, dist: torch.Tensor, local_connectivity: float, bandwidth: float,
+           chunk_rows: int):
+    """a8: (edges int64 (n*k, 2), weights float64 (n*k,)) as smoothen_dists writes them."""
+    _need(idx, "idx", torch.int64, 2)
+    _need(dist, "dist", torch.float32, 2)
+    n, k = idx.shape
+    dev = idx.device
+    edges = torch.empty((n * k, 2), dtype=torch.int64, device=dev)
+    w = torch.empty(n * k, dtype=torch.float64, device=dev)
+    L.check(L.load().sg_smooth(handle(dev.index).ptr, _p(idx), _p(dist), n, k, float(local_connectivity),
+                               float(bandwidth), int(chunk_rows), _p(edges), _p(w), _stream(dev)))
+    return edges, w
+
+
+def fuzzy_union(edges: torch.Tensor, w: torch.Tensor, n: int, k: int, use_k: Optional[int] = None,
+                mix: float = 1.0, upper_only: bool = False) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+    """a9: CSR (indptr int64, indices int32, data float64) of the fuzzy union."""
+    _need(edges, "edges", torch.int64, 2)
+    _need(w, "w", torch.float64, 1)
+    dev = edges.device
+    nnz = edges.shape[0]
+    cap = max(1, 2 * nnz)
+    indptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    ind = torch.empty(cap, dtype=torch.int32, device=dev)
+    dat = torch.empty(cap, dtype=torch.float64, device=dev)
+    L.check(L.load().sg_fuzzy_union(handle(dev.index).ptr, _p(edges), _p(w), nnz, int(n), int(k),
+                                    int(k if use_k is None else use_k), float(mix),
+                                    L.SG_UNION_UPPER_ONLY if upper_only else 0, _p(indptr), _p(ind), _p(dat), cap,
+                                    _stream(dev)))
+    nz = int(indptr[-1].item())
+    return indptr, ind[:nz], dat[:nz]

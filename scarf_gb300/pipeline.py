@@ -1,0 +1,172 @@
+"""The make_graph hot path on one GPU, from CSR counts to the smoothed graph.
+
+normalise (+ column sums) -> z-statistics -> scatter -> FP64 eigh -> projection
+-> exact self-kNN (+ self removal, recall) -> smoothing, all resident in HBM.
+The CSR may be given as host arrays (copied in, optionally streamed in chunks
+of cells from pinned memory with the copy of chunk i+1 overlapping the
+normalisation of chunk i) or as CUDA tensors.
+
+Step order and parameters follow DataStore.make_graph
+(scarf/datastore/graph_datastore.py:513-1020).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import kernels as K
+
+PLAIN_MARGIN = 0
+PRECISION_MARGIN = 16
+
+
+@dataclass
+class GraphResult:
+    n_cells: int
+    n_feats: int
+    dims: int
+    k: int
+    x: Optional[torch.Tensor]          # normalised rows (n x ld), float32
+    mu: torch.Tensor                   # float64
+    sigma: torch.Tensor                # float64
+    mu32: torch.Tensor
+    sigma32: torch.Tensor
+    components: torch.Tensor           # h x (dims+1) float64
+    loadings32: torch.Tensor           # h x dims float32
+    evals: torch.Tensor
+    evr: torch.Tensor
+    scores: torch.Tensor               # n x ld_s float32
+    indices: torch.Tensor              # n x k int64
+    distances: torch.Tensor            # n x k float32
+    n_missed: torch.Tensor             # device int64
+    edges: Optional[torch.Tensor] = None
+    weights: Optional[torch.Tensor] = None
+    timings: dict = field(default_factory=dict)
+
+    @property
+    def loadings(self) -> torch.Tensor:
+        return self.components[:, : self.dims]
+
+    def recall(self) -> float:
+        return 100.0 * (self.n_cells - int(self.n_missed.item())) / self.n_cells
+
+
+def _to_device(a, dtype, dev, stream=None):
+    if isinstance(a, torch.Tensor):
+        t = a
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(a))
+    if t.dtype != dtype:
+        t = t.to(dtype)
+    return t.to(dev, non_blocking=True)
+
+
+def col_map(feat_idx, n_genes: int, device) -> torch.Tensor:
+    m = np.full(n_genes, -1, dtype=np.int32)
+    m[np.asarray(feat_idx)] = np.arange(len(feat_idx), dtype=np.int32)
+    return torch.from_numpy(m).to(device)
+
+
+def normalize_csr_host(indptr, indices, data, n_genes: int, feat_idx, *, size_factor=1000.0,
+                       log_transform=True, renormalize_subset=True, n_counts=None, chunk_cells=None,
+                       device="cuda", missing_mask=None, fill_value=1.0, cmap=None):
+    """a1+a3 over host (ideally pinned) CSR arrays. With ``chunk_cells`` the rows
+    are streamed: chunk i+1 is copied on a side stream while chunk i is
+    normalised. Returns ``(x, colsum, colsumsq)``."""
+    dev = torch.device(device)
+    h = len(feat_idx)
+    n = len(indptr) - 1
+    cmap = col_map(feat_idx, n_genes, dev) if cmap is None else cmap
+    ld = K.round_up(h, 4)
+    x = torch.empty((n, ld), dtype=torch.float32, device=dev)
+    cs = torch.zeros(h, dtype=torch.float64, device=dev)
+    cq = torch.zeros_like(cs)
+    nc = None if n_counts is None else _to_device(n_counts, torch.float64, dev)
+    mm = None if missing_mask is None else _to_device(missing_mask, torch.uint8, dev)
+    ip_h = torch.as_tensor(np.asarray(indptr, dtype=np.int64)) if not isinstance(indptr, torch.Tensor) else indptr
+    ind_h = torch.as_tensor(indices) if not isinstance(indices, torch.Tensor) else indices
+    dat_h = torch.as_tensor(data) if not isinstance(data, torch.Tensor) else data
+    if ind_h.dtype != torch.int32:
+        ind_h = ind_h.to(torch.int32)
+    if dat_h.dtype != torch.int32:
+        dat_h = dat_h.to(torch.int32)
+    if not chunk_cells or chunk_cells >= n:
+        ip = ip_h.to(dev, non_blocking=True)
+        ind = ind_h.to(dev, non_blocking=True)
+        dat = dat_h.to(dev, non_blocking=True)
+        K.normalize_csr(ip, ind, dat, cmap, h, size_factor=size_factor, log_transform=log_transform,
+                        renormalize_subset=renormalize_subset, n_counts=nc, missing_mask=mm, fill_value=fill_value,
+                        out=x, colsum=cs, colsumsq=cq)
+        return x, cs, cq
+    comp = torch.cuda.current_stream(dev)
+    side = torch.cuda.Stream(dev)
+    ipn = ip_h.numpy() if ip_h.device.type == "cpu" else ip_h.cpu().numpy()
+    bounds = list(range(0, n, chunk_cells)) + [n]
+    staged = []
+
+    def stage(ci):
+        a, b = bounds[ci], bounds[ci + 1]
+        pa, pb = int(ipn[a]), int(ipn[b])
+        with torch.cuda.stream(side):
+            t_ip = ip_h[a:b + 1].to(dev, non_blocking=True)
+            t_ind = ind_h[pa:pb].to(dev, non_blocking=True)
+            t_dat = dat_h[pa:pb].to(dev, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(side)
+        return a, b, t_ip, t_ind, t_dat, ev
+
+    nxt = stage(0)
+    for ci in range(len(bounds) - 1):
+        a, b, t_ip, t_ind, t_dat, ev = nxt
+        comp.wait_event(ev)
+        if ci + 2 < len(bounds):
+            nxt = stage(ci + 1)
+        K.normalize_csr(t_ip, t_ind, t_dat, cmap, h, size_factor=size_factor, log_transform=log_transform,
+                        renormalize_subset=renormalize_subset,
+                        n_counts=None if nc is None else nc[a:b], missing_mask=mm, fill_value=fill_value,
+                        out=x[a:b], colsum=cs, colsumsq=cq)
+        for t in (t_ip, t_ind, t_dat):
+            t.record_stream(comp)
+        staged.append((t_ip, t_ind, t_dat))
+        if len(staged) > 2:
+            staged.pop(0)
+    return x, cs, cq
+
+
+def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k: int = 11, *,
+               batch_size: int = 1000, precision: str = "plain", margin: Optional[int] = None,
+               local_connectivity: float = 1.0, bandwidth: float = 1.5, size_factor: float = 1000.0,
+               log_transform: bool = True, renormalize_subset: bool = True, n_counts=None,
+               use_for_pca: Optional[np.ndarray] = None, chunk_cells: Optional[int] = None,
+               smooth: bool = True, keep_x: bool = True, device="cuda") -> GraphResult:
+    """The whole path on the device; returns device tensors."""
+    dev = torch.device(device)
+    n = len(indptr) - 1
+    h = len(feat_idx)
+    # AnnStream caps (scarf/ann.py:91-92, :173-185)
+    k = min(k, n - 1)
+    dims = min(dims, n, batch_size - 1, h - 1)
+    x, cs, cq = normalize_csr_host(indptr, indices, data, n_genes, feat_idx, size_factor=size_factor,
+                                   log_transform=log_transform, renormalize_subset=renormalize_subset,
+                                   n_counts=n_counts, chunk_cells=chunk_cells, device=dev)
+    mu, sigma, mu32, sigma32 = K.zstats(cs, cq, n)
+    mask = None
+    n_used = n
+    if use_for_pca is not None and not np.all(use_for_pca):
+        mask = _to_device(np.asarray(use_for_pca, dtype=np.uint8), torch.uint8, dev)
+        n_used = int(np.count_nonzero(use_for_pca))
+    cov, zsum = K.covariance(x, mu32, sigma32, n_cols=h, row_mask=mask, precision=precision)
+    comps, evals, evr, l32 = K.pca_basis(cov, zsum, n_used, dims + 1, n_load=dims, ld_l=dims)
+    scores = K.project(x, mu32, sigma32, l32, dims, n_cols=h)
+    if margin is None:
+        margin = PRECISION_MARGIN if precision == "precision" else PLAIN_MARGIN
+    idx, dist, nm = K.knn(scores, scores, dims, k, self_offset=0, margin=margin, precision=precision)
+    res = GraphResult(n_cells=n, n_feats=h, dims=dims, k=k, x=x if keep_x else None, mu=mu, sigma=sigma,
+                      mu32=mu32, sigma32=sigma32, components=comps, loadings32=l32, evals=evals, evr=evr,
+                      scores=scores, indices=idx, distances=dist, n_missed=nm)
+    if smooth:
+        res.edges, res.weights = K.smooth(idx, dist, local_connectivity, bandwidth, batch_size)
+    return res

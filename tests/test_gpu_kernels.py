@@ -1,0 +1,278 @@
+"""Parity of each CUDA kernel group (through the C ABI) with the CPU oracle.
+
+Tolerances: integer, index and edge outputs are compared bit-exactly; FP32
+values against the FP64 oracle to the bounds stated in each test; the fuzzy
+union, computed in FP64 with scipy's operation order, bit-exactly.
+"""
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle
+from helpers import clustered_points, small_counts, top_var_genes
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def K():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from scarf_gb300 import kernels
+    return kernels
+
+
+def cu(a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.cuda()
+
+
+@pytest.fixture(scope="module")
+def counts():
+    indptr, indices, data, G, lab = small_counts()
+    feat = top_var_genes(indptr, indices, data, G, 400)
+    return indptr, indices, data, G, feat
+
+
+def _normalize(K, counts, **kw):
+    indptr, indices, data, G, feat = counts
+    cmap = np.full(G, -1, np.int32)
+    cmap[feat] = np.arange(len(feat), dtype=np.int32)
+    h = len(feat)
+    cs = torch.zeros(h, dtype=torch.float64, device="cuda")
+    cq = torch.zeros_like(cs)
+    lib = torch.zeros(len(indptr) - 1, dtype=torch.int64, device="cuda")
+    x = K.normalize_csr(cu(indptr), cu(indices), cu(data), cu(cmap), h, colsum=cs, colsumsq=cq, libsize=lib, **kw)
+    torch.cuda.synchronize()
+    return x, cs, cq, lib
+
+
+def test_normalize_and_stats(K, counts):
+    indptr, indices, data, G, feat = counts
+    x, cs, cq, lib = _normalize(K, counts)
+    want, scal = oracle.normed_csr(indptr, indices, data, G, feat)
+    got = x[:, :len(feat)].double().cpu().numpy()
+    assert np.abs(got - want).max() <= 4e-7 * max(1.0, np.abs(want).max())
+    assert np.array_equal(lib.cpu().numpy(), scal.astype(np.int64))          # integer library sizes, exact
+    assert np.allclose(cs.cpu().numpy(), want.sum(0), rtol=2e-6, atol=1e-6)
+    assert np.allclose(cq.cpu().numpy(), (want ** 2).sum(0), rtol=2e-6, atol=1e-6)
+    mu, sg, mu32, sg32 = K.zstats(cs, cq, len(indptr) - 1)
+    omu, osg = oracle.zstats(want)
+    assert np.allclose(mu.cpu().numpy(), omu, rtol=2e-6, atol=1e-7)
+    assert np.allclose(sg.cpu().numpy(), osg, rtol=2e-6, atol=1e-7)
+
+
+def test_normalize_is_deterministic(K, counts):
+    a = _normalize(K, counts)
+    b = _normalize(K, counts)
+    assert torch.equal(a[0], b[0]) and torch.equal(a[1], b[1]) and torch.equal(a[2], b[2])
+
+
+def test_normalize_modes(K, counts):
+    indptr, indices, data, G, feat = counts
+    ncounts = np.add.reduceat(data.astype(np.int64), indptr[:-1]).astype(np.float64)
+    ncounts[np.diff(indptr) == 0] = 0
+    ncounts[ncounts == 0] = 1.0
+    x, *_ = _normalize(K, counts, renormalize_subset=False, n_counts=cu(ncounts), log_transform=False)
+    want, _ = oracle.normed_csr(indptr, indices, data, G, feat, log_transform=False, renormalize_subset=False,
+                                n_counts=ncounts)
+    got = x[:, :len(feat)].double().cpu().numpy()
+    assert np.allclose(got, want, rtol=4e-7, atol=1e-6)
+    # missing features take the fill value (mapping_utils.py:208 fills 1.0)
+    miss = np.zeros(len(feat), np.uint8)
+    miss[[0, 7, 100]] = 1
+    x2, *_ = _normalize(K, counts, missing_mask=cu(miss), fill_value=1.0)
+    g2 = x2[:, :len(feat)].cpu().numpy()
+    assert np.all(g2[:, [0, 7, 100]] == 1.0)
+    # bf16 output is the rounding of the float32 values
+    x3, *_ = _normalize(K, counts, out_dtype=torch.bfloat16)
+    x1, *_ = _normalize(K, counts)
+    assert torch.equal(x3[:, :len(feat)], x1[:, :len(feat)].to(torch.bfloat16))
+
+
+def _zscaled(counts):
+    indptr, indices, data, G, feat = counts
+    want, _ = oracle.normed_csr(indptr, indices, data, G, feat)
+    mu, sg = oracle.zstats(want)
+    return want, mu, sg, (want - mu) / sg
+
+
+def test_covariance_plain(K, counts):
+    x, cs, cq, _ = _normalize(K, counts)
+    mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
+    xw, omu, osg, z = _zscaled(counts)
+    h = z.shape[1]
+    cov, zsum = K.covariance(x, mu32, sg32, n_cols=h)
+    torch.cuda.synchronize()
+    want = z.T @ z
+    got = cov.cpu().numpy()
+    assert np.abs(got - want).max() <= 2e-5 * np.abs(want).max()
+    assert np.allclose(got, got.T)
+    assert np.abs(zsum.cpu().numpy() - z.sum(0)).max() < 1e-2
+    # row mask
+    mask = (np.arange(x.shape[0]) % 3 != 0).astype(np.uint8)
+    cov2, zs2 = K.covariance(x, mu32, sg32, n_cols=h, row_mask=cu(mask))
+    zm = z[mask.astype(bool)]
+    assert np.abs(cov2.cpu().numpy() - zm.T @ zm).max() <= 2e-5 * np.abs(want).max()
+    assert np.allclose(zs2.cpu().numpy(), zm.sum(0), atol=1e-2)
+
+
+def test_pca_basis_and_projection(K, counts):
+    x, cs, cq, _ = _normalize(K, counts)
+    mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
+    xw, omu, osg, z = _zscaled(counts)
+    h = z.shape[1]
+    dims = 20
+    cov, zsum = K.covariance(x, mu32, sg32, n_cols=h)
+    comps, evals, evr, l32 = K.pca_basis(cov, zsum, x.shape[0], dims + 1, n_load=dims, ld_l=dims)
+    ocomp, oev = oracle.pca_exact(z, dims + 1)
+    ang = oracle.subspace_angles(comps.cpu().numpy()[:, :dims], ocomp[:, :dims])
+    assert ang.max() < 1e-3
+    assert np.allclose(evals.cpu().numpy(), oev, rtol=1e-4)
+    # svd_flip convention: the largest-magnitude entry of each component is positive
+    c = comps.cpu().numpy()
+    assert np.all(c[np.argmax(np.abs(c), 0), np.arange(c.shape[1])] > 0)
+    # leading, well separated components agree one by one
+    for j in range(3):
+        assert np.abs(c[:, j] - ocomp[:, j]).max() < 1e-3
+    scores = K.project(x, mu32, sg32, l32, dims, n_cols=h)
+    torch.cuda.synchronize()
+    want = oracle.reducer(xw, omu, osg, c[:, :dims])
+    got = scores[:, :dims].cpu().numpy()
+    assert np.abs(got - want).max() <= 1e-4 * max(1.0, np.abs(want).max())
+    assert torch.all(scores[:, dims:] == 0)
+
+
+def _self_knn(K, pts, k, **kw):
+    t = cu(np.pad(pts, ((0, 0), (0, (-pts.shape[1]) % 4))))
+    idx, dist, nm = K.knn(t, t, pts.shape[1], k, self_offset=0, **kw)
+    torch.cuda.synchronize()
+    return idx.cpu().numpy(), dist.cpu().numpy(), int(nm.item())
+
+
+@pytest.mark.parametrize("n,d,k", [(3000, 30, 11), (1234, 50, 21), (700, 7, 3)])
+def test_self_knn_plain(K, n, d, k):
+    pts = clustered_points(n, d, seed=n, dup=((5, 6), (10, 11), (10, 12)))
+    gi, gd, nm = _self_knn(K, pts, k)
+    oi, od, rec = oracle.self_query_knn(pts, k, chunk_size=1000)
+    # the self-removal rule counts the same misses (duplicates make self non-first)
+    assert nm == round((100 - rec) * n / 100)
+    # tie-aware recall against the FP64 exact neighbours
+    _, ed = oracle.exact_knn(pts.astype(np.float64), pts.astype(np.float64), k + 1)
+    r = oracle.recall_at_k(pts, pts, gi, od[:, -1])
+    assert r >= 0.999
+    assert np.abs(gd - od).max() <= 1e-4 * max(1.0, od.max())
+    # indices agree except where distances tie within float32 resolution
+    diff = gi != oi
+    if diff.any():
+        assert np.all(np.abs(gd[diff] - od[diff]) <= 1e-4 * np.maximum(1.0, od[diff]))
+
+
+def test_knn_query_mapping(K):
+    refs = clustered_points(5000, 30, seed=1)
+    q = clustered_points(333, 30, seed=2)
+    tr = cu(np.pad(refs, ((0, 0), (0, 2))))
+    tq = cu(np.pad(q, ((0, 0), (0, 2))))
+    idx, dist, _ = K.knn(tq, tr, 30, 7)
+    torch.cuda.synchronize()
+    oi, od = oracle.exact_knn(q, refs, 7)
+    assert oracle.recall_at_k(q, refs, idx.cpu().numpy(), od[:, -1]) >= 0.999
+    assert np.abs(dist.cpu().numpy() - od).max() <= 1e-4 * max(1.0, od.max())
+
+
+def test_knn_edges(K):
+    # k + 1 == n, a single query, ragged sizes
+    pts = clustered_points(9, 5, seed=3)
+    gi, gd, nm = _self_knn(K, pts, 8)
+    oi, od, rec = oracle.self_query_knn(pts, 8)
+    assert np.array_equal(np.sort(gi, 1), np.sort(oi.astype(np.int64), 1))
+    refs = clustered_points(131, 5, seed=4)
+    q = refs[:1].copy()
+    idx, dist, _ = K.knn(cu(np.pad(q, ((0, 0), (0, 3)))), cu(np.pad(refs, ((0, 0), (0, 3)))), 5, 4)
+    oi, od = oracle.exact_knn(q, refs, 4)
+    assert np.array_equal(idx.cpu().numpy(), oi)
+    with pytest.raises(ValueError):
+        K.knn(cu(np.pad(q, ((0, 0), (0, 3)))), cu(np.pad(refs, ((0, 0), (0, 3)))), 5, 200)
+
+
+def test_knn_many_splits(K):
+    # few queries against many references: the reference range is split across CTAs
+    refs = clustered_points(60000, 16, seed=5)
+    q = clustered_points(50, 16, seed=6)
+    idx, dist, _ = K.knn(cu(q), cu(refs), 16, 11)
+    oi, od = oracle.exact_knn(q, refs, 11)
+    assert oracle.recall_at_k(q, refs, idx.cpu().numpy(), od[:, -1]) >= 0.999
+
+
+def test_smooth_known_answer(K, golden_dir):
+    kat = np.load(os.path.join(golden_dir, "pbmc1k_knn.npz"))
+    idx = cu(kat["indices"].astype(np.int64))
+    dist = cu(kat["distances"].astype(np.float32))
+    edges, w = K.smooth(idx, dist, 1.0, 1.5, 1000)
+    torch.cuda.synchronize()
+    n, k = kat["indices"].shape
+    e = edges.cpu().numpy()
+    assert np.array_equal(e[:, 0], np.repeat(np.arange(n), k))
+    assert np.array_equal(e[:, 1], kat["indices"].ravel().astype(np.int64))
+    assert np.abs(w.cpu().numpy() - kat["weights"]).max() < 1e-5
+
+
+def test_smooth_chunked_global_min(K, golden_dir):
+    ref = np.load(os.path.join(golden_dir, "ref_functions.npz"))
+    idx = cu(ref["smooth_idx"].astype(np.int64))
+    dist = cu(ref["smooth_dist"].astype(np.float32))
+    edges, w = K.smooth(idx, dist, 1.0, 1.5, int(ref["smooth_chunk"]))
+    torch.cuda.synchronize()
+    assert np.array_equal(edges.cpu().numpy(), ref["smooth_edges"].astype(np.int64))
+    got = w.cpu().numpy()
+    want = ref["smooth_w"]
+    assert np.array_equal(got == want.min(), want == want.min())  # the same zero positions were fixed
+    assert np.abs(got - want).max() < 1e-5
+
+
+def test_smooth_vs_oracle_random(K):
+    pts = clustered_points(2500, 12, seed=9, dup=((1, 2),))
+    oi, od, _ = oracle.self_query_knn(pts, 15)
+    for chunk in (1000, 333):
+        edges, w = K.smooth(cu(oi.astype(np.int64)), cu(od.astype(np.float32)), 1.0, 1.5, chunk)
+        e, ow = oracle.smoothen_dists(oi, od, 1.0, 1.5, chunk)
+        assert np.array_equal(edges.cpu().numpy(), e.astype(np.int64))
+        assert np.abs(w.cpu().numpy() - ow).max() < 1e-5
+
+
+def _csr(ref, p):
+    return ref[p + "_indptr"], ref[p + "_indices"], ref[p + "_data"]
+
+
+def test_fuzzy_union_bit_exact(K, golden_dir):
+    ref = np.load(os.path.join(golden_dir, "ref_functions.npz"))
+    n = int(ref["union_n"])
+    edges = np.stack([ref["union_rows"], ref["union_cols"]], 1).astype(np.int64)
+    k = edges.shape[0] // n
+    for mix, p in ((1.0, "sym"), (1.0, "fss"), (0.7, "fss07")):
+        ip, ind, dat = K.fuzzy_union(cu(edges), cu(ref["union_w"]), n, k, mix=mix)
+        for got, want in zip((ip, ind, dat), _csr(ref, p)):
+            assert np.array_equal(got.cpu().numpy(), want)
+
+
+def test_fuzzy_union_use_k_upper_and_hubs(K):
+    rng = np.random.default_rng(11)
+    n, k = 3000, 9
+    cols = rng.integers(0, n, size=(n, k))
+    cols[:, 0] = 17              # a hub: in-degree 3000 exercises the CTA sorter
+    cols[::5, 1] = 999           # a second, smaller hub
+    w = rng.random(n * k).astype(np.float32).astype(np.float64)
+    edges = np.stack([np.repeat(np.arange(n), k), cols.ravel()], 1).astype(np.int64)
+    for use_k, upper in ((k, False), (4, False), (k, True)):
+        g = oracle.store_to_sparse(edges, w, n, k, use_k)
+        want = oracle.symmetrize(g, upper_only=upper)
+        want.sort_indices()
+        ip, ind, dat = K.fuzzy_union(cu(edges), cu(w), n, k, use_k=use_k, upper_only=upper)
+        assert np.array_equal(ip.cpu().numpy(), want.indptr)
+        assert np.array_equal(ind.cpu().numpy(), want.indices)
+        assert np.array_equal(dat.cpu().numpy(), want.data)
