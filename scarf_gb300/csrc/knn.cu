@@ -16,9 +16,9 @@
 
 #include <algorithm>
 
-int sg_knn_candidates_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs, int64_t nr, int d,
-                         int ld, int kc, bool self, int* cand, int nsplit_max, int* nsplit_out, int* lists_out,
-                         cudaStream_t st);  // knn_tc.cu
+int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs, int64_t nr, int d, int ld, int kq,
+              int k, int64_t self_offset, int margin, int64_t* idx_out, float* dist_out, unsigned long long* nmiss,
+              cudaStream_t st);  // knn_tc.cu
 
 namespace {
 
@@ -326,6 +326,11 @@ extern "C" int sg_knn(sg_handle* h, const float* queries, int64_t nq, const floa
   SG_ARG(kq <= nr, "sg_knn: %d neighbours requested from %lld references", kq, (long long)nr);
   SG_ARG(kq <= 64, "sg_knn: k=%d too large (k + self <= 64)", k);
   if (nq == 0) return SG_OK;
+  if (precision == SG_PRECISION) {
+    unsigned long long* nm_p = reinterpret_cast<unsigned long long*>(n_missed);
+    return sg_knn_tc(h, queries, nq, refs, nr, d, ld, kq, k, self_offset, margin, idx_out, dist_out,
+                     self ? nm_p : nullptr, st);
+  }
   int kc = kq + margin;
   kc = kc <= 16 ? 16 : kc <= 32 ? 32 : 64;
   SG_ARG(kq + margin <= 64, "sg_knn: k + margin too large (<= 64 candidates per list)");
@@ -356,10 +361,7 @@ extern "C" int sg_knn(sg_handle* h, const float* queries, int64_t nq, const floa
   int* cand = cv.take<int>(size_t(nsplit) * 2 * nq_pad * kc);
   unsigned long long* nm = cv.take<unsigned long long>(1);
 
-  int nlists = 2 * nsplit;
-  if (precision == SG_PRECISION) {
-    return sg::fail(SG_ERR_UNSUPPORTED, "sg_knn: the precision form is not built yet");
-  }
+  const int nlists = 2 * nsplit;
   transpose_pad_kernel<<<sg::ceil_div_i(nr_pad, 256), 256, 0, st>>>(refs, nr, d, ld, RT, nr_pad, rn);
   SG_LAUNCH_CHECK();
   if (!same) {
