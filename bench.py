@@ -1,0 +1,433 @@
+#!/usr/bin/env python
+"""make_graph throughput of scarf's graph-construction path on GB300.
+
+Workload (default, ``--config c2``): 100,000 cells x 30,000 genes of seeded
+negative-binomial counts (20 clusters), 2,000 HVGs, 50 PCs, k = 21, smoothing
+chunks of 1,000 rows. One step = normalise -> z-stats -> scatter -> FP64 eigh
+-> projection -> self-kNN (+ self removal) -> smoothing over the whole matrix.
+
+* ``value``: cells/s of the precision form (BF16 tcgen05 distances + FP32
+  re-rank of k+1+16 candidates) with the CSR already resident in HBM.
+* ``e2e``: the same through the public pipeline call with pinned HOST CSR,
+  host->device copies and the device->host read of indices, distances, edges
+  and weights inside every timed step.
+* ``plain``: the all-FP32 form on the same input.
+* ``--impl reference``: the CPU restatement of the reference path (the
+  oracle), timed on a bounded sample of the same workload on the host cores.
+
+Launch: ``python bench.py [--gpus N --steps K --warmup W]``; N > 1 runs under
+torchrun as N independent replicas (the path is one GPU per graph).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    "c1": dict(name="C1: 10,000 cells x 20,000 genes NB (8 clusters), 2,000 HVGs, 30 PCs, k=11",
+               n_cells=10_000, n_genes=20_000, n_clusters=8, n_hvg=2000, dims=30, k=11, lib_median=3000.0),
+    "c2": dict(name="C2: 100,000 cells x 30,000 genes NB (20 clusters), 2,000 HVGs, 50 PCs, k=21",
+               n_cells=100_000, n_genes=30_000, n_clusters=20, n_hvg=2000, dims=50, k=21, lib_median=3000.0),
+    "c3": dict(name="C3: 1,000,000 cells x 30,000 genes NB (40 clusters), 2,000 HVGs, 50 PCs, k=21, "
+                    "50,000-cell chunks from pinned host memory",
+               n_cells=1_000_000, n_genes=30_000, n_clusters=40, n_hvg=2000, dims=50, k=21, lib_median=2500.0,
+               chunk=50_000),
+}
+BATCH = 1000
+SEED = 4466
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def make_input(cfg, device):
+    from scarf_gb300 import synth
+    csr = synth.nb_counts(cfg["n_cells"], cfg["n_genes"], cfg["n_clusters"], SEED, lib_median=cfg["lib_median"],
+                          device=device, chunk=4096)
+    feat = synth.select_hvgs(csr, cfg["n_hvg"])
+    return csr, feat
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+def traffic_table():
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+def kernel_work(cfg, nnz):
+    """Algorithmic work of one launch of each kernel at this workload."""
+    n, h, d, k = cfg["n_cells"], cfg["n_hvg"], cfg["dims"], cfg["k"]
+    return {
+        "normalize": ("hbm", 8.0 * nnz + 8.0 * (n + 1) + 4.0 * n * h),
+        "cov_simt": ("fp32", 2.0 * n * h * h),
+        "project": ("fp32", 2.0 * n * h * d),
+        "knn_tc": ("tensor", 2.0 * n * n * d),
+        "knn_simt": ("fp32", 2.0 * n * n * d),
+        "rerank": ("fp32", 2.0 * n * (k + 1 + 16) * d),
+        "smooth": ("hbm", n * k * (8.0 + 4.0) + n * k * (16.0 + 8.0)),
+    }
+
+
+# ---------------------------------------------------------------------------
+def recall_sample(scores, idx, d, k, n_sample=2000, seed=0):
+    """Tie-aware recall@k of the returned neighbours against exact FP64 kNN of
+    the same scores for a seeded sample of query rows (computed on the GPU)."""
+    import torch
+    n = scores.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    rows = torch.randperm(n, generator=g)[:min(n_sample, n)].to(scores.device)
+    s = scores[:, :d].double()
+    q = s[rows]
+    d2 = (q * q).sum(1, keepdim=True) + (s * s).sum(1)[None, :] - 2.0 * q @ s.T
+    d2[torch.arange(len(rows), device=s.device), rows] = float("inf")   # self removed
+    kth = torch.topk(d2, k, dim=1, largest=False).values[:, -1]
+    got = idx[rows]
+    diff = q[:, None, :] - s[got]
+    dg = (diff * diff).sum(-1)
+    hit = dg <= kth[:, None] * (1 + 1e-6) + 1e-12
+    return float(hit.double().mean().item())
+
+
+def run_gb300(args, cfg):
+    import torch
+    import torch.distributed as dist
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl")
+    import __graft_entry__
+    __graft_entry__.build()
+    from scarf_gb300 import kernels as K
+    from scarf_gb300 import pipeline
+
+    dev = torch.device("cuda", local)
+    csr, feat = make_input(cfg, dev)
+    n, G = csr.n_cells, csr.n_genes
+    dims, k = cfg["dims"], cfg["k"]
+    chunk = cfg.get("chunk")
+    ip_h = torch.from_numpy(csr.indptr).pin_memory()
+    ind_h = torch.from_numpy(csr.indices).pin_memory()
+    dat_h = torch.from_numpy(csr.data).pin_memory()
+    ip_d, ind_d, dat_d = ip_h.to(dev), ind_h.to(dev), dat_h.to(dev)
+    torch.cuda.synchronize()
+
+    def step(form, host=False, outs=None):
+        if host:
+            res = pipeline.make_graph(ip_h, ind_h, dat_h, G, feat, dims, k, batch_size=BATCH, precision=form,
+                                      chunk_cells=chunk, keep_x=False)
+            # the step's result read back to the host
+            for name in ("indices", "distances", "edges", "weights"):
+                outs[name].copy_(getattr(res, name), non_blocking=True)
+            return res
+        return pipeline.make_graph(ip_d, ind_d, dat_d, G, feat, dims, k, batch_size=BATCH, precision=form,
+                                   keep_x=False)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(form, steps, warmup, host=False, prof=False):
+        outs = None
+        if host:
+            outs = {"indices": torch.empty((n, k), dtype=torch.int64).pin_memory(),
+                    "distances": torch.empty((n, k), dtype=torch.float32).pin_memory(),
+                    "edges": torch.empty((n * k, 2), dtype=torch.int64).pin_memory(),
+                    "weights": torch.empty(n * k, dtype=torch.float64).pin_memory()}
+        res = None
+        for _ in range(warmup):
+            res = step(form, host, outs)
+        barrier()
+        if prof:
+            K.profile(True)
+            K.profile_reset()
+        l0 = K.kernel_launches()
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            res = step(form, host, outs)
+        e1.record(st)
+        barrier()
+        launches = K.kernel_launches() - l0
+        ms = e0.elapsed_time(e1) / steps
+        prof_ms = {}
+        if prof:
+            for name in ("normalize", "cov_simt", "eigh", "project", "knn_tc", "knn_simt", "rerank", "smooth"):
+                t, c = K.profile_query(name)
+                if c:
+                    prof_ms[name] = (t / c, c / steps)
+            K.profile(False)
+        if ws > 1:
+            t = torch.tensor([ms], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, res, launches, prof_ms, outs
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms, res, launches, prof_ms, _ = timed("precision", args.steps, args.warmup, prof=True)
+    clocks = sampler.stop()
+    rec = recall_sample(res.scores, res.indices, res.dims, res.k)
+    ann_recall = res.recall()
+    e2e_ms, res_h, _, _, outs = timed("precision", args.steps, max(1, min(args.warmup, 2)), host=True)
+    plain_ms, res_p, _, prof_p, _ = timed("plain", max(1, min(args.steps, 3)), 1, prof=True)
+    rec_p = recall_sample(res_p.scores, res_p.indices, res_p.dims, res_p.k)
+    # the two forms produce the same graph up to near-ties
+    same_nbr = float((res_p.indices == res.indices).double().mean().item())
+    w_diff = float((res_p.weights - res.weights).abs().max().item())
+
+    pk = peaks()
+    work = kernel_work(cfg, csr.nnz)
+    kernels = {}
+    for name, (t, per_step) in prof_ms.items():
+        kind, amount = work.get(name, (None, None))
+        ent = {"ms": round(t, 4), "launches_per_step": per_step}
+        if kind == "hbm":
+            ent["GB/s"] = round(amount / (t * 1e-3) / 1e9, 1)
+        elif kind in ("tensor", "fp32"):
+            ent["TFLOP/s"] = round(amount / (t * 1e-3) / 1e12, 2)
+        kernels[name] = ent
+    top = max(prof_ms.items(), key=lambda kv: kv[1][0])[0] if prof_ms else None
+    roof = None
+    tt = traffic_table()
+    if top is not None:
+        kind, amount = work.get(top, ("tensor", 0.0))
+        t = prof_ms[top][0] * 1e-3
+        if kind == "hbm":
+            ach, peak, unit = amount / t / 1e9, pk["hbm_gbs"], "GB/s"
+        else:
+            ach, peak, unit = amount / t / 1e12, pk["bf16_tflops"], "TFLOP/s"
+        tr = tt.get(f"{args.config}:{top}")
+        roof = {"kernel": top, "bound": "hbm" if kind == "hbm" else "tensor", "achieved": round(ach, 2),
+                "peak": peak, "unit": unit, "frac": round(ach / peak, 4),
+                "traffic": tr, "peak_source": pk["source"] + " (MEASURED_PEAKS.json, burst)",
+                "work_per_launch": amount}
+    h2d = int(ip_h.numel() * 8 + ind_h.numel() * 4 + dat_h.numel() * 4)
+    d2h = int(sum(v.numel() * v.element_size() for v in outs.values()))
+    cells = n * ws
+    line = {
+        "metric": "make_graph cells/s",
+        "value": round(cells / (ms * 1e-3), 1),
+        "unit": "cells/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16",
+        "data": "synthetic (seeded negative-binomial counts generated on the device)",
+        "config": {"workload": cfg["name"], "form": "precision: bf16 tcgen05 distances, f32 re-rank, "
+                   "f32 normalise/scatter/projection, f64 eigh", "margin": 16, "batch_size": BATCH,
+                   "nnz": csr.nnz, "l2": "inputs larger than L2 (CSR %.2f GB, normalised matrix %.2f GB)"
+                   % (h2d / 1e9, n * cfg["n_hvg"] * 4 / 1e9), "parallelism": f"replicas x{ws}"},
+        "recall_at_k": round(rec, 5),
+        "ann_recall_pct": round(ann_recall, 3),
+        "plain": {"value": round(cells / (plain_ms * 1e-3), 1), "ms_per_step": round(plain_ms, 3),
+                  "recall_at_k": round(rec_p, 5), "speedup_precision_vs_plain": round(plain_ms / ms, 3),
+                  "same_neighbour_frac": round(same_nbr, 5), "max_weight_diff": w_diff,
+                  "kernels_ms": {k_: round(v[0], 4) for k_, v in prof_p.items()}},
+        "kernels": kernels,
+        "e2e": {"value": round(cells / (e2e_ms * 1e-3), 1), "unit": "cells/s", "ms_per_step": round(e2e_ms, 3),
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": roof,
+        "clocks": clocks,
+        "gpu_launches": int(launches),
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(csr, feat, cfg, res, big=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+def cpu_reference_times(csr, feat, cfg, rows=2000, ipca_blocks=1, queries=100, seed=0, ref_scores=None):
+    """Per-stage wall times of the CPU restatement on a bounded sample,
+    extrapolated to the whole workload by each stage's cost model (linear in
+    cells for normalisation, statistics, PCA blocks, projection and
+    smoothing; queries x all references for the exact kNN)."""
+    import oracle
+    n, G, dims, k = csr.n_cells, csr.n_genes, cfg["dims"], cfg["k"]
+    rows = min(rows, n)
+    t = {}
+    p = csr.indptr[:rows + 1]
+    t0 = time.perf_counter()
+    x, _ = oracle.normed_csr(p, csr.indices[:p[-1]], csr.data[:p[-1]], G, feat)
+    mu, sg = oracle.zstats(x)
+    t["normalise+stats"] = (time.perf_counter() - t0) * n / rows
+    z = (x - mu) / sg
+    pca = oracle.IncrementalPCARestated(dims + 1)
+    nb = max(1, min(ipca_blocks, rows // BATCH))
+    t0 = time.perf_counter()
+    for b in range(nb):
+        pca.partial_fit(z[b * BATCH:(b + 1) * BATCH])
+    t["pca (IncrementalPCA blocks)"] = (time.perf_counter() - t0) * (n / BATCH) / nb
+    load = pca.components_[:-1].T
+    t0 = time.perf_counter()
+    s = oracle.reducer(x, mu, sg, load)
+    t["projection x2"] = 2 * (time.perf_counter() - t0) * n / rows
+    if ref_scores is None:
+        rng = np.random.default_rng(seed)
+        ref_scores = rng.normal(size=(n, dims)).astype(np.float32)
+    q = np.asarray(ref_scores[:queries], dtype=np.float64)
+    t0 = time.perf_counter()
+    ki, kd = oracle.exact_knn(q, ref_scores, k + 1)
+    fi, fd, _ = oracle.fix_knn_query(ki, kd.astype(np.float32), np.arange(queries))
+    t["exact kNN (stand-in for hnswlib)"] = (time.perf_counter() - t0) * n / queries
+    t0 = time.perf_counter()
+    oracle.smoothen_dists(fi.astype(np.uint64), fd.astype(np.float64), 1.0, 1.5, BATCH)
+    t["smoothing"] = (time.perf_counter() - t0) * n / queries
+    return t, s
+
+
+def cpu_baseline(csr, feat, cfg, res=None, big=False):
+    ref = None
+    if res is not None:
+        ref = res.scores[:, :res.dims].float().cpu().numpy()
+    kw = dict(rows=10_000, ipca_blocks=4, queries=1000) if big else dict(rows=2000, ipca_blocks=1, queries=100)
+    t, _ = cpu_reference_times(csr, feat, cfg, ref_scores=ref, **kw)
+    total = sum(t.values())
+    return {"value": round(csr.n_cells / total, 2), "unit": "cells/s", "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": (f"oracle (numpy/scipy restatement) on {kw['rows']} cells for normalise/stats/projection, "
+                       f"{kw['ipca_blocks']} IncrementalPCA blocks of {BATCH}, {kw['queries']} exact-kNN queries "
+                       f"against all {csr.n_cells} references, smoothing of those rows; each stage scaled to "
+                       f"{csr.n_cells} cells; BLAS on all cores, the rest single-threaded numpy"),
+            "stage_seconds_projected": {k_: round(v, 3) for k_, v in t.items()}}
+
+
+def run_reference(args, cfg):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    csr, feat = make_input(cfg, dev)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        t, _ = cpu_reference_times(csr, feat, cfg, seed=i)
+        if i >= args.warmup:
+            vals.append(sum(t.values()))
+    total = statistics.median(vals)
+    v = round(csr.n_cells / total, 2)
+    print(json.dumps({
+        "impl": "reference", "metric": "make_graph cells/s", "value": v, "unit": "cells/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total * 1e3, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (same seeded input)",
+        "config": {"workload": cfg["name"], "form": "reference CPU restatement"},
+        "cpu_baseline": {"value": v, "unit": "cells/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "per step: 2000 cells normalise/stats/projection, 1 IncrementalPCA block, "
+                                   "100 exact-kNN queries against all references, smoothing of those rows; "
+                                   "scaled to the full workload"},
+        "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup) if args.impl == "gb300" else args.warmup
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        run_reference(args, cfg)
+    else:
+        run_gb300(args, cfg)
+
+
+if __name__ == "__main__":
+    main()

@@ -56,6 +56,17 @@ int sg_destroy(sg_handle* h);
 /* Bytes of scratch the handle holds now. */
 size_t sg_workspace_bytes(const sg_handle* h);
 
+/* Diagnostics (no reference counterpart): number of this library's kernels
+ * launched by the process so far; per-kernel device time measured with CUDA
+ * events around the named launches while profiling is on. Names:
+ * "normalize", "cov_simt", "cov_tc", "project", "knn_simt", "knn_tc",
+ * "rerank", "smooth", "union". sg_profile_query synchronises the recorded
+ * events. */
+unsigned long long sg_kernel_launches(void);
+int sg_profile(sg_handle* h, int enable);
+int sg_profile_reset(sg_handle* h);
+int sg_profile_query(sg_handle* h, const char* name, double* total_ms, long long* count);
+
 /* a1+a3 -- library-size normalisation of CSR counts with the feature gather,
  * fused with the column sums of the written values.
  * Replaces RNAassay.normed (scarf/assay.py:780-828) with norm_lib_size /

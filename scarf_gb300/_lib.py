@@ -42,6 +42,10 @@ SIGNATURES = {
     "sg_create": (C.c_int, [C.c_int, sz, C.POINTER(vp)]),
     "sg_destroy": (C.c_int, [vp]),
     "sg_workspace_bytes": (sz, [vp]),
+    "sg_kernel_launches": (C.c_ulonglong, []),
+    "sg_profile": (C.c_int, [vp, C.c_int]),
+    "sg_profile_reset": (C.c_int, [vp]),
+    "sg_profile_query": (C.c_int, [vp, C.c_char_p, C.POINTER(f64), C.POINTER(C.c_longlong)]),
     "sg_normalize_csr": (C.c_int, [vp, vp, vp, vp, i64, vp, i64, i32, vp, f32, vp, f64, u32, vp, i64, i32, vp,
                                    vp, vp, vp]),
     "sg_zstats": (C.c_int, [vp, vp, vp, i64, i32, vp, vp, vp, vp, vp]),

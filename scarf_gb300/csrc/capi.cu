@@ -1,17 +1,40 @@
 // Handle, error and scratch management of the C ABI.
 #include "common.cuh"
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 
 namespace {
 thread_local char g_err[1024] = {0};
+std::atomic<unsigned long long> g_launches{0};
+
+void prof_drain(sg_handle* h) {
+  for (auto& r : h->prof_pending) {
+    float ms = 0.f;
+    cudaEventSynchronize(r.b);
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    bool found = false;
+    for (auto& s : h->prof_done)
+      if (strcmp(s.name, r.name) == 0) {
+        s.ms += ms;
+        s.count += 1;
+        found = true;
+      }
+    if (!found) h->prof_done.push_back({r.name, double(ms), 1});
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  h->prof_pending.clear();
 }
+}  // namespace
 
 namespace sg {
 
 void clear_error() { g_err[0] = 0; }
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 int fail(int status, const char* fmt, ...) {
   va_list ap;
@@ -97,6 +120,7 @@ int sg_create(int device, size_t hbm_budget_bytes, sg_handle** out) {
 int sg_destroy(sg_handle* h) {
   if (!h) return SG_OK;
   cudaSetDevice(h->device);
+  prof_drain(h);
   sg_solver_destroy(h);
   if (h->ws) cudaFree(h->ws);
   delete h;
@@ -104,5 +128,37 @@ int sg_destroy(sg_handle* h) {
 }
 
 size_t sg_workspace_bytes(const sg_handle* h) { return h ? h->ws_bytes : 0; }
+
+unsigned long long sg_kernel_launches(void) { return g_launches.load(); }
+
+int sg_profile(sg_handle* h, int enable) {
+  if (!h) return sg::fail(SG_ERR_ARG, "null sg_handle");
+  cudaSetDevice(h->device);
+  prof_drain(h);
+  h->prof = enable != 0;
+  return SG_OK;
+}
+
+int sg_profile_reset(sg_handle* h) {
+  if (!h) return sg::fail(SG_ERR_ARG, "null sg_handle");
+  cudaSetDevice(h->device);
+  prof_drain(h);
+  h->prof_done.clear();
+  return SG_OK;
+}
+
+int sg_profile_query(sg_handle* h, const char* name, double* total_ms, long long* count) {
+  if (!h || !name || !total_ms || !count) return sg::fail(SG_ERR_ARG, "sg_profile_query: null argument");
+  cudaSetDevice(h->device);
+  prof_drain(h);
+  *total_ms = 0.0;
+  *count = 0;
+  for (auto& s : h->prof_done)
+    if (strcmp(s.name, name) == 0) {
+      *total_ms = s.ms;
+      *count = s.count;
+    }
+  return SG_OK;
+}
 
 }  // extern "C"

@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <cstddef>
+#include <vector>
 
 #include "../../include/scarf_gb300.h"
 
@@ -19,11 +20,43 @@ struct sg_handle {
   void* solver = nullptr;    // cusolverDnHandle_t, created on first use
   void* solver_work = nullptr;
   size_t solver_work_bytes = 0;
+  // kernel timing (off unless sg_profile(h, 1)): events around named launches
+  bool prof = false;
+  struct ProfRec {
+    const char* name;
+    cudaEvent_t a, b;
+  };
+  std::vector<ProfRec> prof_pending;
+  struct ProfSum {
+    const char* name;
+    double ms;
+    int64_t count;
+  };
+  std::vector<ProfSum> prof_done;
 };
 
 namespace sg {
 
 int fail(int status, const char* fmt, ...);
+void count_launch();
+
+// Times the launches issued on `st` while in scope when the handle profiles.
+struct ProfScope {
+  sg_handle* h;
+  const char* name;
+  cudaStream_t st;
+  cudaEvent_t a = nullptr, b = nullptr;
+  ProfScope(sg_handle* h_, const char* n, cudaStream_t s) : h(h_), name(n), st(s) {
+    if (h && h->prof && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess)
+      cudaEventRecord(a, st);
+  }
+  ~ProfScope() {
+    if (a && b) {
+      cudaEventRecord(b, st);
+      h->prof_pending.push_back({name, a, b});
+    }
+  }
+};
 int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
 void clear_error();
 
@@ -61,7 +94,11 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
     if (e_ != cudaSuccess) return sg::cuda_fail(e_, #call, __FILE__, __LINE__); \
   } while (0)
 
-#define SG_LAUNCH_CHECK() SG_CUDA(cudaGetLastError())
+#define SG_LAUNCH_CHECK()  \
+  do {                     \
+    SG_CUDA(cudaGetLastError()); \
+    sg::count_launch();    \
+  } while (0)
 
 #define SG_HANDLE_CHECK(h)                                            \
   do {                                                                \

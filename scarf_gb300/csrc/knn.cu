@@ -369,10 +369,14 @@ extern "C" int sg_knn(sg_handle* h, const float* queries, int64_t nq, const floa
     SG_LAUNCH_CHECK();
   }
   int rc;
+  {
+  sg::ProfScope prof(h, "knn_simt", st);
   if (kc == 16) rc = launch_simt<16>(QT, nq_pad, RT, nr_pad, rn, d, nq, nr, rps, nsplit, cand, nq_pad, st);
   else if (kc == 32) rc = launch_simt<32>(QT, nq_pad, RT, nr_pad, rn, d, nq, nr, rps, nsplit, cand, nq_pad, st);
   else rc = launch_simt<64>(QT, nq_pad, RT, nr_pad, rn, d, nq, nr, rps, nsplit, cand, nq_pad, st);
+  }
   if (rc != SG_OK) return rc;
+  sg::ProfScope prof(h, "rerank", st);
   unsigned long long* nmiss = self ? reinterpret_cast<unsigned long long*>(n_missed) : nm;
   return sg_rerank(queries, refs, d, ld, nq, cand, nlists, kc, nq_pad, kq, k, self_offset, idx_out, dist_out, nmiss, st);
 }

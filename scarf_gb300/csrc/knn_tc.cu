@@ -427,15 +427,19 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   if (rc) return rc;
   rc = make_map(&tb, Rb, nr_pad, BN);
   if (rc) return rc;
+  {
+  sg::ProfScope prof(h, "knn_tc", st);
   if (kc == 16) rc = launch_tc<16>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, err, st);
   else if (kc == 32) rc = launch_tc<32>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, err, st);
   else if (kc == 48) rc = launch_tc<48>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, err, st);
   else rc = launch_tc<64>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, err, st);
+  }
   if (rc) return rc;
   int herr = 0;
   SG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
   SG_CUDA(cudaStreamSynchronize(st));
   if (herr) return sg::fail(SG_ERR_TIMEOUT, "sg_knn: a tensor-core pipeline wait expired (stage %d)", herr);
+  sg::ProfScope prof(h, "rerank", st);
   return sg_rerank(queries, refs, d, ld, nq, cand, nsplit, kc, nq_pad, kq, k, self_offset, idx_out, dist_out, nmiss,
                    st);
 }

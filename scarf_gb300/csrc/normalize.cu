@@ -248,6 +248,7 @@ extern "C" int sg_normalize_csr(sg_handle* h, const int64_t* indptr, const int32
     gq = cv.take<double>(size_t(ngroups) * n_cols);
   }
   const float sf = float(size_factor);
+  sg::ProfScope prof(h, "normalize", st);
   if (out_dtype == SG_F32) {
     SG_CUDA(cudaFuncSetAttribute(normalize_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     normalize_kernel<false><<<nblocks, nwarps * 32, smem, st>>>(

@@ -341,6 +341,7 @@ extern "C" int sg_covariance(sg_handle* h, const float* x, int64_t n_rows, int32
   float* part = cv.take<float>(size_t(nsplit) * n_pad * n_pad);
   float* zpart = cv.take<float>(size_t(nsplit) * n_pad);
   dim3 grid(ntile, nsplit);
+  sg::ProfScope prof(h, "cov_simt", st);
   cov_simt_kernel<<<grid, 256, 0, st>>>(x, n_rows, n_cols, ld, mu32, sigma32, row_mask, T, rows_per_split, part,
                                         n_pad, zpart);
   SG_LAUNCH_CHECK();
@@ -397,6 +398,7 @@ extern "C" int sg_pca_basis(sg_handle* h, const double* cov, const double* zsum,
     SG_CUDA(cudaMalloc(&h->solver_work, wbytes));
     h->solver_work_bytes = wbytes;
   }
+  sg::ProfScope prof(h, "eigh", st);
   cusolverStatus_t cs = cusolverDnDsyevdx(sol, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER, n,
                                           A, n, 0.0, 0.0, il, iu, &meig, W, static_cast<double*>(h->solver_work), lwork,
                                           info);
@@ -423,6 +425,7 @@ extern "C" int sg_project(sg_handle* h, const float* x, int64_t n_rows, int32_t 
   SG_ARG(!bf16_out || ld_b >= d, "sg_project: ld_b < d");
   if (n_rows == 0) return SG_OK;
   const int ccols = std::max<int>(ld_s, bf16_out ? ld_b : 0);
+  sg::ProfScope prof(h, "project", st);
   dim3 grid(sg::ceil_div_i(n_rows, PR), sg::ceil_div_i(std::min<int>(ccols, sg::ceil_div_i(d, PC) * PC), PC));
   project_kernel<<<grid, 256, 0, st>>>(x, n_rows, n_cols, ld, mu32, sigma32, loadings32, d, ld_l, scores, ld_s,
                                        static_cast<__nv_bfloat16*>(bf16_out), ld_b);

@@ -211,6 +211,7 @@ extern "C" int sg_smooth(sg_handle* h, const int64_t* knn_idx, const float* knn_
   const double target = log2(double(k)) * bandwidth;
   const size_t smem = sizeof(float) * kRowsPerCta * (k + 1);
   SG_CUDA(cudaFuncSetAttribute(smooth_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  sg::ProfScope prof(h, "smooth", st);
   smooth_kernel<<<sg::ceil_div_i(n, kRowsPerCta), kRowsPerCta, smem, st>>>(
       knn_idx, knn_dist, n, k, local_connectivity, target, chunk_rows, csum, edges_out, w_out, w32, cmin,
       czero);

@@ -270,6 +270,7 @@ extern "C" int sg_fuzzy_union(sg_handle* h, const int64_t* edges, const double* 
   int* nbig = cv.take<int>(1);
   unsigned long long* bad = cv.take<unsigned long long>(1);
 
+  sg::ProfScope prof(h, "union", st);
   SG_CUDA(cudaMemsetAsync(deg, 0, sizeof(int) * n, st));
   SG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int) * n, st));
   SG_CUDA(cudaMemsetAsync(nbig, 0, sizeof(int), st));

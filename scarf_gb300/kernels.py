@@ -253,3 +253,25 @@ def fuzzy_union(edges: torch.Tensor, w: torch.Tensor, n: int, k: int, use_k: Opt
                                     _stream(dev)))
     nz = int(indptr[-1].item())
     return indptr, ind[:nz], dat[:nz]
+
+
+# --------------------------------------------------------------------------
+def kernel_launches() -> int:
+    """Number of this library's kernels launched by the process so far."""
+    return int(L.load().sg_kernel_launches())
+
+
+def profile(enable: bool, device: Optional[int] = None) -> None:
+    L.check(L.load().sg_profile(handle(device).ptr, 1 if enable else 0))
+
+
+def profile_reset(device: Optional[int] = None) -> None:
+    L.check(L.load().sg_profile_reset(handle(device).ptr))
+
+
+def profile_query(name: str, device: Optional[int] = None) -> Tuple[float, int]:
+    """(total device ms, launches) of the named kernel while profiling was on."""
+    ms = C.c_double()
+    cnt = C.c_longlong()
+    L.check(L.load().sg_profile_query(handle(device).ptr, name.encode(), C.byref(ms), C.byref(cnt)))
+    return ms.value, cnt.value

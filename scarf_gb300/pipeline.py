@@ -21,6 +21,8 @@ from . import kernels as K
 
 PLAIN_MARGIN = 0
 PRECISION_MARGIN = 16
+# covariance forms with a kernel in this build
+COV_FORMS = ("plain",)
 
 
 @dataclass
@@ -141,8 +143,12 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k:
                local_connectivity: float = 1.0, bandwidth: float = 1.5, size_factor: float = 1000.0,
                log_transform: bool = True, renormalize_subset: bool = True, n_counts=None,
                use_for_pca: Optional[np.ndarray] = None, chunk_cells: Optional[int] = None,
-               smooth: bool = True, keep_x: bool = True, device="cuda") -> GraphResult:
-    """The whole path on the device; returns device tensors."""
+               smooth: bool = True, keep_x: bool = True, cov_form: Optional[str] = None,
+               device="cuda") -> GraphResult:
+    """The whole path on the device; returns device tensors.
+
+    ``precision`` selects the kNN form; ``cov_form`` the covariance form
+    (default: the same as ``precision`` where that form is built)."""
     dev = torch.device(device)
     n = len(indptr) - 1
     h = len(feat_idx)
@@ -158,7 +164,9 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k:
     if use_for_pca is not None and not np.all(use_for_pca):
         mask = _to_device(np.asarray(use_for_pca, dtype=np.uint8), torch.uint8, dev)
         n_used = int(np.count_nonzero(use_for_pca))
-    cov, zsum = K.covariance(x, mu32, sigma32, n_cols=h, row_mask=mask, precision=precision)
+    if cov_form is None:
+        cov_form = precision if precision in COV_FORMS else "plain"
+    cov, zsum = K.covariance(x, mu32, sigma32, n_cols=h, row_mask=mask, precision=cov_form)
     comps, evals, evr, l32 = K.pca_basis(cov, zsum, n_used, dims + 1, n_load=dims, ld_l=dims)
     scores = K.project(x, mu32, sigma32, l32, dims, n_cols=h)
     if margin is None:
