@@ -420,13 +420,34 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--mode", default="full", choices=["full", "step"],
+                    help="step: warm-up steps then one make_graph step and nothing else (for profilers)")
+    ap.add_argument("--form", default="precision", choices=["precision", "plain"], help="form used by --mode step")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "gb300" else args.warmup
     cfg = CONFIGS[args.config]
     if args.impl == "reference":
         run_reference(args, cfg)
+    elif args.mode == "step":
+        run_step(args, cfg)
     else:
         run_gb300(args, cfg)
+
+
+def run_step(args, cfg):
+    """W warm-up steps and one step of one form, CSR resident on the device."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from scarf_gb300 import pipeline
+    dev = torch.device("cuda", 0)
+    csr, feat = make_input(cfg, dev)
+    ip, ind, dat = (torch.from_numpy(a).to(dev) for a in (csr.indptr, csr.indices, csr.data))
+    for _ in range(args.warmup + 1):
+        res = pipeline.make_graph(ip, ind, dat, csr.n_genes, feat, cfg["dims"], cfg["k"], batch_size=BATCH,
+                                  precision=args.form, keep_x=False)
+    torch.cuda.synchronize()
+    print(json.dumps({"mode": "step", "config": args.config, "form": args.form, "ann_recall_pct": res.recall()}))
 
 
 if __name__ == "__main__":

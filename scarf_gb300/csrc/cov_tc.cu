@@ -1,9 +1,259 @@
 // a4, precision form: 3xBF16 split covariance on the tcgen05 tensor cores.
-#include "common.cuh"
+//
+// zsplit: z = (x - mu)/sigma in float32 (rows outside the PCA mask are 0),
+//   split into hi = bf16(z) and lo = bf16(z - hi), and written transposed
+//   (feature-major, cells contiguous: the K-major operand layout), with
+//   per-tile column sums of z for the centring term.
+// gemm: D[128 x 256] tile of Z^T Z for the tiles that touch the upper
+//   triangle, K = a split of the cells in steps of 64; per step three
+//   products hi.hi + hi.lo + lo.hi (12 tcgen05.mma kind::f16 K=16) accumulate
+//   in one FP32 TMEM accumulator fed by a 2-stage TMA ring (4 tiles per stage).
+//   Each CTA writes its FP32 partial tile; partials are reduced over the
+//   splits in FP64 in a fixed order by the reduction of pca.cu.
+#include "tc_ptx.cuh"
+
+namespace {
+
+using namespace tc;
+
+constexpr int BM = 128;
+constexpr int BN = 256;
+constexpr int BK = 64;
+constexpr int STAGES = 2;
+constexpr uint32_t A_BYTES = BM * BK * 2;
+constexpr uint32_t B_BYTES = BN * BK * 2;
+constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+constexpr uint32_t TMEM_COLS = 256;
+constexpr size_t SMEM_BYTES = 1024 + size_t(STAGES) * STAGE_BYTES + 256;
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
+constexpr int ZT = 64;  // zsplit tile
+
+__global__ void __launch_bounds__(256)
+zsplit_kernel(const float* __restrict__ x, int64_t n_rows, int n_cols, int64_t ld, const float* __restrict__ mu,
+              const float* __restrict__ sg, const uint8_t* __restrict__ mask, __nv_bfloat16* __restrict__ hi,
+              __nv_bfloat16* __restrict__ lo, int64_t n_pad, float* __restrict__ zpart, int h_pad) {
+  __shared__ float t[ZT][ZT + 1];
+  const int64_t r0 = int64_t(blockIdx.x) * ZT;
+  const int c0 = blockIdx.y * ZT;
+  const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;  // 64 x 4
+  for (int rr = ty; rr < ZT; rr += 4) {
+    const int64_t r = r0 + rr;
+    const int c = c0 + tx;
+    float z = 0.f;
+    if (r < n_rows && c < n_cols && (mask == nullptr || mask[r] != 0)) z = __fdiv_rn(x[r * ld + c] - mu[c], sg[c]);
+    t[rr][tx] = z;
+  }
+  __syncthreads();
+  // column sums of z over this row tile
+  if (threadIdx.x < ZT) {
+    float s = 0.f;
+    for (int rr = 0; rr < ZT; ++rr) s += t[rr][threadIdx.x];
+    zpart[int64_t(blockIdx.x) * h_pad + c0 + threadIdx.x] = s;
+  }
+  // transposed, split writes: feature c, cells r0..r0+63
+  for (int cc = ty; cc < ZT; cc += 4) {
+    const float z = t[tx][cc];
+    const __nv_bfloat16 h = __float2bfloat16_rn(z);
+    const __nv_bfloat16 l = __float2bfloat16_rn(z - __bfloat162float(h));
+    const int64_t o = int64_t(c0 + cc) * n_pad + r0 + tx;
+    hi[o] = h;
+    lo[o] = l;
+  }
+}
+
+// tile t of the 128 x 256 tiles whose column block reaches the diagonal
+__device__ __forceinline__ int2 cov_tile(int t, int TI, int TJ) {
+  for (int i = 0; i < TI; ++i) {
+    const int j0 = (i * BM) / BN;
+    const int cnt = TJ - j0;
+    if (t < cnt) return make_int2(i, j0 + t);
+    t -= cnt;
+  }
+  return make_int2(TI - 1, TJ - 1);
+}
+
+__global__ void __launch_bounds__(192, 1)
+cov_tc_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+              const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, int TI, int TJ,
+              int64_t steps_per_split, int64_t total_steps, float* __restrict__ part, int n_pad, int* __restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = su32(smem_raw);
+  uint8_t* sm = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + STAGES * STAGE_BYTES);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + STAGES;
+  uint64_t* acc_full = bars + 2 * STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_full + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int2 tile = cov_tile(blockIdx.x, TI, TJ);
+  const int64_t k_begin = int64_t(blockIdx.y) * steps_per_split;
+  const int64_t k_end = min(total_steps, k_begin + steps_per_split);
+  const int nsteps = int(k_end - k_begin);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(acc_full, 1);
+    fence_barrier_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(tmem_slot, TMEM_COLS);
+    tmem_relinquish();
+  }
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      tma_prefetch(&mAh);
+      tma_prefetch(&mAl);
+      tma_prefetch(&mBh);
+      tma_prefetch(&mBl);
+      int issued = 0;
+      for (int t = 0; t < nsteps; ++t) {
+        const int s = t % STAGES;
+        const uint32_t ph = (t / STAGES) & 1;
+        if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) break;
+        uint8_t* st = sm + s * STAGE_BYTES;
+        const int kx = int((k_begin + t) * BK);
+        mbar_expect_tx(&full[s], STAGE_BYTES);
+        tma_load_2d(st, &mAh, &full[s], kx, tile.x * BM);
+        tma_load_2d(st + A_BYTES, &mAl, &full[s], kx, tile.x * BM);
+        tma_load_2d(st + 2 * A_BYTES, &mBh, &full[s], kx, tile.y * BN);
+        tma_load_2d(st + 2 * A_BYTES + B_BYTES, &mBl, &full[s], kx, tile.y * BN);
+        ++issued;
+      }
+      if (*reinterpret_cast<volatile int*>(err)) {
+        for (int t = max(0, issued - STAGES); t < issued; ++t)
+          for (uint32_t it = 0; it < WAIT_LIMIT && !mbar_try_wait(&full[t % STAGES], (t / STAGES) & 1); ++it) {
+          }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int issued = 0;
+      for (int t = 0; t < nsteps; ++t) {
+        const int s = t % STAGES;
+        const uint32_t ph = (t / STAGES) & 1;
+        if (!mbar_wait(&full[s], ph, err, 2)) break;
+        tc_fence_after();
+        uint8_t* st = sm + s * STAGE_BYTES;
+        const uint64_t ah = smem_desc_sw128(su32(st));
+        const uint64_t al = smem_desc_sw128(su32(st + A_BYTES));
+        const uint64_t bh = smem_desc_sw128(su32(st + 2 * A_BYTES));
+        const uint64_t bl = smem_desc_sw128(su32(st + 2 * A_BYTES + B_BYTES));
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk) {
+          const uint64_t o = uint64_t(2 * kk);
+          mma_bf16(tmem, ah + o, bh + o, kIdesc, (t > 0 || kk > 0) ? 1u : 0u);
+          mma_bf16(tmem, ah + o, bl + o, kIdesc, 1u);
+          mma_bf16(tmem, al + o, bh + o, kIdesc, 1u);
+        }
+        mma_commit(&empty[s]);
+        ++issued;
+      }
+      mma_commit(acc_full);  // arrives once every MMA issued above has completed
+      (void)issued;
+    }
+  } else {
+    const int quarter = warp & 3;
+    const int row = quarter * 32 + lane;
+    const bool ok = mbar_wait(acc_full, 0, err, 3);
+    if (__all_sync(0xffffffffu, ok)) {
+      tc_fence_after();
+      float* P = part + int64_t(blockIdx.y) * n_pad * n_pad + int64_t(tile.x * BM + row) * n_pad + tile.y * BN;
+      const uint32_t tbase = tmem + (uint32_t(quarter * 32) << 16);
+#pragma unroll 1
+      for (int ch = 0; ch < BN / 32; ++ch) {
+        uint32_t r[32];
+        tmem_ld32(tbase + uint32_t(ch * 32), r);
+        tmem_wait_ld(r);
+        float4* o = reinterpret_cast<float4*>(P + ch * 32);
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          o[q] = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]), __uint_as_float(r[4 * q + 2]),
+                             __uint_as_float(r[4 * q + 3]));
+      }
+    }
+    tc_fence_before();
+  }
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+__global__ void zpart_reduce_kernel(const float* __restrict__ zpart, int ntiles, int h_pad, int n_cols,
+                                    double* __restrict__ zsum) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_cols) return;
+  double s = 0.0;
+  for (int t = 0; t < ntiles; ++t) s += double(zpart[int64_t(t) * h_pad + j]);
+  zsum[j] += s;
+}
+
+}  // namespace
+
+// pca.cu: FP64 reduction of split partials over the 128 x 128 upper tiles
+int sg_cov_reduce(const float* part, int nsplit, int n_pad, int n_cols, double* cov, cudaStream_t st);
 
 int sg_covariance_tc(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld, const float* mu32,
                      const float* sigma32, const uint8_t* row_mask, double* cov, double* zsum, cudaStream_t st) {
-  (void)h; (void)x; (void)n_rows; (void)n_cols; (void)ld; (void)mu32; (void)sigma32; (void)row_mask; (void)cov;
-  (void)zsum; (void)st;
-  return sg::fail(SG_ERR_UNSUPPORTED, "sg_covariance: the precision form is not built yet");
+  const int h_pad = int(sg::ceil_div(n_cols, BN) * BN);
+  const int64_t n_pad = sg::ceil_div(n_rows, BK) * BK;
+  const int64_t total_steps = n_pad / BK;
+  if (n_pad >= (int64_t(1) << 31)) return sg::fail(SG_ERR_ARG, "sg_covariance: too many rows for one call");
+  const int TI = h_pad / BM, TJ = h_pad / BN;
+  int ntile = 0;
+  for (int i = 0; i < TI; ++i) ntile += TJ - (i * BM) / BN;
+  // K splits: enough CTAs for several waves, at least 8 steps each
+  int64_t want = std::max<int64_t>(1, (int64_t(h->sm_count) * 6 + ntile - 1) / ntile);
+  int64_t sps = std::max<int64_t>(8, sg::ceil_div(total_steps, want));
+  const int nsplit = int(sg::ceil_div(total_steps, sps));
+  const int zt = int(n_pad / ZT);
+  const size_t need = 2 * sg::Carver::need(size_t(h_pad) * n_pad * 2) +
+                      sg::Carver::need(size_t(nsplit) * h_pad * h_pad * 4) + sg::Carver::need(size_t(zt) * h_pad * 4) +
+                      sg::Carver::need(sizeof(int));
+  int status;
+  void* w = sg::ws_get(h, need, &status);
+  if (!w) return status;
+  sg::Carver cv(w);
+  __nv_bfloat16* zh = cv.take<__nv_bfloat16>(size_t(h_pad) * n_pad);
+  __nv_bfloat16* zl = cv.take<__nv_bfloat16>(size_t(h_pad) * n_pad);
+  float* part = cv.take<float>(size_t(nsplit) * h_pad * h_pad);
+  float* zpart = cv.take<float>(size_t(zt) * h_pad);
+  int* err = cv.take<int>(1);
+  SG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+  {
+    sg::ProfScope prof(h, "zsplit", st);
+    zsplit_kernel<<<dim3(unsigned(zt), unsigned(h_pad / ZT)), 256, 0, st>>>(x, n_rows, n_cols, ld, mu32, sigma32,
+                                                                          row_mask, zh, zl, n_pad, zpart, h_pad);
+    SG_LAUNCH_CHECK();
+  }
+  CUtensorMap mAh, mAl, mBh, mBl;
+  int rc = make_map(&mAh, zh, h_pad, BM, n_pad, BK);
+  if (!rc) rc = make_map(&mAl, zl, h_pad, BM, n_pad, BK);
+  if (!rc) rc = make_map(&mBh, zh, h_pad, BN, n_pad, BK);
+  if (!rc) rc = make_map(&mBl, zl, h_pad, BN, n_pad, BK);
+  if (rc) return rc;
+  {
+    sg::ProfScope prof(h, "cov_tc", st);
+    SG_CUDA(cudaFuncSetAttribute(cov_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SMEM_BYTES)));
+    cov_tc_kernel<<<dim3(unsigned(ntile), unsigned(nsplit)), 192, SMEM_BYTES, st>>>(mAh, mAl, mBh, mBl, TI, TJ, sps,
+                                                                                 total_steps, part, h_pad, err);
+    SG_LAUNCH_CHECK();
+  }
+  int herr = 0;
+  SG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(cudaStreamSynchronize(st));
+  if (herr) return sg::fail(SG_ERR_TIMEOUT, "sg_covariance: a tensor-core pipeline wait expired (stage %d)", herr);
+  rc = sg_cov_reduce(part, nsplit, h_pad, n_cols, cov, st);
+  if (rc) return rc;
+  zpart_reduce_kernel<<<sg::ceil_div_i(n_cols, 256), 256, 0, st>>>(zpart, zt, h_pad, n_cols, zsum);
+  SG_LAUNCH_CHECK();
+  return SG_OK;
 }

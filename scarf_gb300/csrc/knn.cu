@@ -26,6 +26,7 @@ constexpr int QT_ = 128;  // queries per CTA
 constexpr int RT_ = 128;  // refs per tile
 constexpr int DS_PITCH = RT_ + 4;
 constexpr int kMaxD = 64;
+constexpr int BUFS = 24;  // candidate buffer slots per (query row, half)
 
 template <int KC>
 struct TopK {
@@ -97,9 +98,22 @@ knn_simt_kernel(const float* __restrict__ QT, int64_t ldq, const float* __restri
   const int64_t s_begin = int64_t(blockIdx.y) * refs_per_split;
   const int64_t s_end = min(nr, s_begin + refs_per_split);
   const int my_row = tid & 127, half = tid >> 7;
+  float* bk = Ns + 2 * RT_ + tid;                                  // slot s: bk[s * 256]
+  int* bi = reinterpret_cast<int*>(Ns + 2 * RT_ + BUFS * 256) + tid;
 
   TopK<KC> top;
   top.init();
+  float thr = __int_as_float(0x7f800000);
+  int cnt = 0;
+  // merge the buffered candidates into the sorted register list
+  auto compact = [&]() {
+    for (int s2 = 0; s2 < cnt; ++s2) {
+      const float v = bk[s2 * 256];
+      if (v < top.worst()) top.insert(v, bi[s2 * 256]);
+    }
+    cnt = 0;
+    thr = top.worst();
+  };
 
   // queries once
   for (int e = tid; e < d * (QT_ / 4); e += 256) {
@@ -158,22 +172,31 @@ knn_simt_kernel(const float* __restrict__ QT, int64_t ldq, const float* __restri
       *reinterpret_cast<float4*>(&Ds[row * DS_PITCH + 64 + tx * 4]) = make_float4(o[4], o[5], o[6], o[7]);
     }
     __syncthreads();
-    // phase 2: scan this thread's half row
+    // phase 2: filter this thread's half row into its candidate buffer
     const float* D = Ds + my_row * DS_PITCH + half * 64;
     const int base = int(r0) + half * 64;
-#pragma unroll 4
-    for (int c = 0; c < 64; c += 4) {
-      const float4 v = *reinterpret_cast<const float4*>(&D[c]);
-      const float thr = top.worst();
-      if (fminf(fminf(v.x, v.y), fminf(v.z, v.w)) < thr) {
-        if (v.x < top.worst()) top.insert(v.x, base + c);
-        if (v.y < top.worst()) top.insert(v.y, base + c + 1);
-        if (v.z < top.worst()) top.insert(v.z, base + c + 2);
-        if (v.w < top.worst()) top.insert(v.w, base + c + 3);
+#pragma unroll 2
+    for (int c = 0; c < 64; c += 8) {
+      if (__any_sync(0xffffffffu, cnt > BUFS - 8)) compact();
+      const float4 v0 = *reinterpret_cast<const float4*>(&D[c]);
+      const float4 v1 = *reinterpret_cast<const float4*>(&D[c + 4]);
+      const float kk[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+      const float m = fminf(fminf(fminf(kk[0], kk[1]), fminf(kk[2], kk[3])),
+                            fminf(fminf(kk[4], kk[5]), fminf(kk[6], kk[7])));
+      if (m < thr) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          if (kk[q] < thr) {
+            bk[cnt * 256] = kk[q];
+            bi[cnt * 256] = base + c + q;
+            ++cnt;
+          }
+        }
       }
     }
     buf ^= 1;
   }
+  compact();
   cp_async_wait_all();
   const int64_t q = q0 + my_row;
   int* out = cand + ((int64_t(blockIdx.y) * 2 + half) * nq_pad + q) * KC;
@@ -279,7 +302,8 @@ rerank_kernel(const float* __restrict__ queries, const float* __restrict__ refs,
 template <int KC>
 int launch_simt(const float* QT, int64_t ldq, const float* RT, int64_t ldr, const float* rn, int d, int64_t nq,
                 int64_t nr, int64_t rps, int nsplit, int* cand, int64_t nq_pad, cudaStream_t st) {
-  const size_t smem = sizeof(float) * (size_t(kMaxD) * QT_ + 2 * size_t(kMaxD) * RT_ + QT_ * DS_PITCH + 2 * RT_);
+  const size_t smem = sizeof(float) * (size_t(kMaxD) * QT_ + 2 * size_t(kMaxD) * RT_ + QT_ * DS_PITCH + 2 * RT_) +
+                      size_t(BUFS) * 256 * 8;
   SG_CUDA(cudaFuncSetAttribute(knn_simt_kernel<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   dim3 grid(unsigned(nq_pad / QT_), unsigned(nsplit));
   knn_simt_kernel<KC><<<grid, 256, smem, st>>>(QT, ldq, RT, ldr, rn, d, nq, nr, rps, cand, nq_pad);

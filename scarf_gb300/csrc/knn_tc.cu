@@ -14,10 +14,7 @@
 // Every mbarrier wait is bounded: on expiry the kernel raises an error flag,
 // drains its own TMA copies and MMAs (again bounded), frees TMEM and returns.
 // The candidates are re-ranked exactly in FP32 by knn.cu.
-#include "common.cuh"
-
-#include <cuda.h>
-#include <cudaTypedefs.h>
+#include "tc_ptx.cuh"
 
 #include <algorithm>
 
@@ -27,114 +24,21 @@ int sg_rerank(const float* queries, const float* refs, int d, int ld, int64_t nq
 
 namespace {
 
+using namespace tc;
+
 constexpr int BM = 128;
 constexpr int BN = 256;
 constexpr int BK = 64;
-constexpr int STAGES = 4;
+constexpr int STAGES = 3;
 constexpr uint32_t A_BYTES = BM * BK * 2;
 constexpr uint32_t B_BYTES = BN * BK * 2;
 constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t WAIT_LIMIT = 1u << 22;
-constexpr size_t SMEM_BYTES = 1024 /*align*/ + A_BYTES + STAGES * B_BYTES + 256 /*barriers*/ + 4 * BN * 4 /*rn*/;
+constexpr int BUF = 64;  // candidate buffer slots per query row
+__host__ __device__ constexpr size_t smem_bytes(int) {
+  return 1024 /*align*/ + A_BYTES + STAGES * B_BYTES + 256 /*barriers*/ + 4 * BN * 4 /*rn*/ +
+         size_t(BUF) * BM * 8 /*buffers*/;
+}
 
-__device__ __forceinline__ uint32_t su32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred P;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, P;\n\t}"
-      : "=r"(ok)
-      : "r"(su32(b)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: false when the limit expires (the error flag is then raised)
-// or when another thread has already raised it.
-__device__ __noinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int* err, int code) {
-  for (uint32_t it = 0;; ++it) {
-    if (mbar_try_wait(b, parity)) return true;
-    if ((it & 255u) == 255u) {
-      if (*reinterpret_cast<volatile int*>(err)) return false;
-      if (it >= WAIT_LIMIT) {
-        atomicCAS(err, 0, code);
-        return false;
-      }
-    }
-  }
-}
-__device__ __forceinline__ void fence_barrier_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, uint64_t* bar, int x, int y) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::
-          "r"(su32(dst)),
-      "l"(reinterpret_cast<uint64_t>(tm)), "r"(su32(bar)), "r"(x), "r"(y)
-      : "memory");
-}
-__device__ __forceinline__ void tma_prefetch(const CUtensorMap* tm) {
-  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tm)) : "memory");
-}
-__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(slot)), "r"(ncols)
-               : "memory");
-}
-__device__ __forceinline__ void tmem_relinquish() {
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred P;\n\t"
-      "setp.ne.b32 P, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, P;\n\t}" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
-// 1024 bytes (stride byte offset), descriptor version 1.
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= uint64_t((saddr & 0x3FFFFu) >> 4);
-  d |= uint64_t(1) << 16;            // leading byte offset (unused for this layout)
-  d |= uint64_t(1024 >> 4) << 32;    // stride byte offset
-  d |= uint64_t(1) << 46;            // version
-  d |= uint64_t(2) << 61;            // SWIZZLE_128B
-  return d;
-}
 // Instruction descriptor, kind::f16: D F32, A/B BF16, both K-major, N, M.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
 
@@ -174,7 +78,7 @@ template <int KC>
 __global__ void __launch_bounds__(192, 1)
 knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const float* __restrict__ rn, int64_t nr, int64_t rps, int* __restrict__ cand, int64_t nq_pad,
-              int* __restrict__ err) {
+              int fold, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = su32(smem_raw);
   uint8_t* sm = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -188,6 +92,8 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   uint64_t* a_full = acc_empty + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(a_full + 1);
   float* rn_s = reinterpret_cast<float*>(sm + A_BYTES + STAGES * B_BYTES + 256);
+  float* bufk = rn_s + 4 * BN;                          // [BUF][BM]
+  int* bufi = reinterpret_cast<int*>(bufk + BUF * BM);  // [BUF][BM]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t q0 = int64_t(blockIdx.x) * BM;
@@ -275,49 +181,85 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
     const int quarter = warp & 3;  // TMEM lanes [32*quarter, 32*quarter+32) are this warp's
     const int row = quarter * 32 + lane;
     float* my_rn = rn_s + (warp - 2) * BN;
+    float* bk = bufk + row;  // slot s of this row's candidate buffer: bk[s * BM]
+    int* bi = bufi + row;
     TopK<KC> top;
     top.init();
+    float thr = __int_as_float(0x7f800000);
+    int cnt = 0;
+    // merge the buffered candidates into the sorted register list
+    auto compact = [&]() {
+      for (int s2 = 0; s2 < cnt; ++s2) {
+        const float v = bk[s2 * BM];
+        if (v < top.worst()) top.insert(v, bi[s2 * BM]);
+      }
+      cnt = 0;
+      thr = top.worst();
+    };
+    // filter one chunk of 32 accumulator columns into the buffer
+    auto process = [&](const uint32_t (&r)[32], int ch, int64_t r0, bool use_rn, int lim) {
+      const int cbase = int(r0) + ch * 32;
+#pragma unroll
+      for (int j = 0; j < 32; j += 8) {
+        float kk[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const float a = __uint_as_float(r[j + q]);
+          float key = use_rn ? fmaf(-2.f, a, my_rn[ch * 32 + j + q]) : a;
+          if (lim < BN && ch * 32 + j + q >= lim) key = __int_as_float(0x7f800000);
+          kk[q] = key;
+        }
+        const float m = fminf(fminf(fminf(kk[0], kk[1]), fminf(kk[2], kk[3])),
+                              fminf(fminf(kk[4], kk[5]), fminf(kk[6], kk[7])));
+        if (m < thr) {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            if (kk[q] < thr) {
+              bk[cnt * BM] = kk[q];
+              bi[cnt * BM] = cbase + j + q;
+              ++cnt;
+            }
+          }
+        }
+      }
+    };
     for (int t = 0; t < ntiles; ++t) {
       const int b = t & 1;
       const uint32_t aph = (t >> 1) & 1;
       const int64_t r0 = s_begin + int64_t(t) * BN;
-      const float4* src = reinterpret_cast<const float4*>(rn + r0);
-      reinterpret_cast<float4*>(my_rn)[lane * 2] = __ldg(src + lane * 2);
-      reinterpret_cast<float4*>(my_rn)[lane * 2 + 1] = __ldg(src + lane * 2 + 1);
+      const int lim = int(min(int64_t(BN), nr - r0));
+      const bool use_rn = !fold;
+      if (use_rn) {
+        const float4* src = reinterpret_cast<const float4*>(rn + r0);
+        reinterpret_cast<float4*>(my_rn)[lane * 2] = __ldg(src + lane * 2);
+        reinterpret_cast<float4*>(my_rn)[lane * 2 + 1] = __ldg(src + lane * 2 + 1);
+      }
       bool ok = mbar_wait(&acc_full[b], aph, err, 5);
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) break;
       tc_fence_after();
       __syncwarp();
       const uint32_t tbase = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(b * BN);
+      uint32_t ra[32], rb[32];
+      tmem_ld32(tbase, ra);
+      tmem_wait_ld(ra);
 #pragma unroll 1
-      for (int ch = 0; ch < BN / 32; ++ch) {
-        uint32_t r[32];
-        __syncwarp();
-        tmem_ld32(tbase + uint32_t(ch * 32), r);
-        tmem_wait_ld();
-        const float* nrm = my_rn + ch * 32;
-        const int cbase = int(r0) + ch * 32;
-#pragma unroll
-        for (int j = 0; j < 32; j += 4) {
-          const float4 nv = *reinterpret_cast<const float4*>(nrm + j);
-          const float k0 = fmaf(-2.f, __uint_as_float(r[j]), nv.x);
-          const float k1 = fmaf(-2.f, __uint_as_float(r[j + 1]), nv.y);
-          const float k2 = fmaf(-2.f, __uint_as_float(r[j + 2]), nv.z);
-          const float k3 = fmaf(-2.f, __uint_as_float(r[j + 3]), nv.w);
-          if (fminf(fminf(k0, k1), fminf(k2, k3)) < top.worst()) {
-            if (k0 < top.worst()) top.insert(k0, cbase + j);
-            if (k1 < top.worst()) top.insert(k1, cbase + j + 1);
-            if (k2 < top.worst()) top.insert(k2, cbase + j + 2);
-            if (k3 < top.worst()) top.insert(k3, cbase + j + 3);
-          }
-        }
+      for (int ch = 0; ch < BN / 32; ch += 2) {
+        tmem_ld32(tbase + uint32_t((ch + 1) * 32), rb);
+        if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
+        process(ra, ch, r0, use_rn, lim);
+        tmem_wait_ld(rb);
+        if (ch + 2 < BN / 32) tmem_ld32(tbase + uint32_t((ch + 2) * 32), ra);
+        if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
+        process(rb, ch + 1, r0, use_rn, lim);
+        if (ch + 2 < BN / 32) tmem_wait_ld(ra);
       }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&acc_empty[b]);
       __syncwarp();
     }
+    compact();
     int* out = cand + (int64_t(blockIdx.y) * nq_pad + q0 + row) * KC;
 #pragma unroll
     for (int j = 0; j < KC; ++j) out[j] = top.i[j];
@@ -329,56 +271,56 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   }
 }
 
-// BF16 copy of float32 rows, zero padded to 64 columns and to n_pad rows;
-// norms are those of the rounded rows (+inf for padding rows).
-__global__ void to_bf16_kernel(const float* __restrict__ in, int64_t n, int d, int ld, __nv_bfloat16* __restrict__ out,
-                               int64_t n_pad, float* __restrict__ norms) {
+// BF16 operands, zero padded to 64 columns and n_pad rows.
+// refs: the rounded rows; with `fold`, columns d, d+1, d+2 carry |r_b|^2 split
+//   into three BF16 terms (hi, mid, lo), so that the product with the query's
+//   ones gives the norm to ~2^-24 relative; norms[] = |r_b|^2 (+inf for padding).
+// queries: -2 * rounded rows (exact in BF16) and, with `fold`, ones in columns
+//   d..d+2. The accumulator is then |r|^2 - 2 q.r directly.
+__global__ void refs_bf16_kernel(const float* __restrict__ in, int64_t n, int d, int ld, int fold,
+                                 __nv_bfloat16* __restrict__ out, int64_t n_pad, float* __restrict__ norms) {
   const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (r >= n_pad) return;
   float s = 0.f;
   __nv_bfloat16* o = out + r * BK;
-  for (int c = 0; c < BK; ++c) {
-    const float v = (r < n && c < d) ? in[r * ld + c] : 0.f;
-    const __nv_bfloat16 b = __float2bfloat16_rn(v);
+  for (int c = 0; c < d; ++c) {
+    const __nv_bfloat16 b = __float2bfloat16_rn(r < n ? in[r * ld + c] : 0.f);
     o[c] = b;
     const float bf = __bfloat162float(b);
     s = fmaf(bf, bf, s);
   }
-  if (norms) norms[r] = r < n ? s : __int_as_float(0x7f800000);
-}
-
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  for (int c = d; c < BK; ++c) o[c] = __float2bfloat16_rn(0.f);
+  if (fold && r < n) {
+    const __nv_bfloat16 hi = __float2bfloat16_rn(s);
+    const float rem1 = s - __bfloat162float(hi);
+    const __nv_bfloat16 mid = __float2bfloat16_rn(rem1);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(rem1 - __bfloat162float(mid));
+    o[d] = hi;
+    o[d + 1] = mid;
+    o[d + 2] = lo;
   }
-  return fn;
+  norms[r] = r < n ? s : __int_as_float(0x7f800000);
 }
 
-int make_map(CUtensorMap* tm, const void* base, int64_t rows, int box_rows) {
-  auto fn = encode_fn();
-  if (!fn) return sg::fail(SG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
-  cuuint64_t gdim[2] = {cuuint64_t(BK), cuuint64_t(rows)};
-  cuuint64_t gstride[1] = {cuuint64_t(BK) * 2};
-  cuuint32_t box[2] = {cuuint32_t(BK), cuuint32_t(box_rows)};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), gdim, gstride, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return sg::fail(SG_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", int(r));
-  return SG_OK;
+__global__ void queries_bf16_kernel(const float* __restrict__ in, int64_t n, int d, int ld, int fold,
+                                    __nv_bfloat16* __restrict__ out, int64_t n_pad) {
+  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= n_pad) return;
+  __nv_bfloat16* o = out + r * BK;
+  for (int c = 0; c < d; ++c) {
+    const float v = __bfloat162float(__float2bfloat16_rn(r < n ? in[r * ld + c] : 0.f));
+    o[c] = __float2bfloat16_rn(-2.f * v);
+  }
+  for (int c = d; c < BK; ++c) o[c] = __float2bfloat16_rn((fold && c < d + 3) ? 1.f : 0.f);
 }
 
 template <int KC>
 int launch_tc(const CUtensorMap& a, const CUtensorMap& b, const float* rn, int64_t nr, int64_t rps, int nsplit,
-              int* cand, int64_t nq_pad, int* err, cudaStream_t st) {
-  SG_CUDA(cudaFuncSetAttribute(knn_tc_kernel<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(SMEM_BYTES)));
+              int* cand, int64_t nq_pad, int fold, int* err, cudaStream_t st) {
+  const size_t smem = smem_bytes(KC);
+  SG_CUDA(cudaFuncSetAttribute(knn_tc_kernel<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   dim3 grid(unsigned(nq_pad / BM), unsigned(nsplit));
-  knn_tc_kernel<KC><<<grid, 192, SMEM_BYTES, st>>>(a, b, rn, nr, rps, cand, nq_pad, err);
+  knn_tc_kernel<KC><<<grid, 192, smem, st>>>(a, b, rn, nr, rps, cand, nq_pad, fold, err);
   SG_LAUNCH_CHECK();
   return SG_OK;
 }
@@ -392,7 +334,7 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   if (d > BK) return sg::fail(SG_ERR_ARG, "sg_knn: the precision form supports d <= %d", BK);
   int kc = kq + margin;
   if (kc > 64) return sg::fail(SG_ERR_ARG, "sg_knn: k + margin too large (<= 64 candidates per list)");
-  kc = kc <= 16 ? 16 : kc <= 32 ? 32 : kc <= 48 ? 48 : 64;
+  kc = kc <= 16 ? 16 : kc <= 32 ? 32 : kc <= 40 ? 40 : kc <= 48 ? 48 : 64;
   const int64_t nq_pad = sg::ceil_div(nq, BM) * BM;
   const int64_t nr_pad = sg::ceil_div(nr, BN) * BN;
   if (nr_pad >= (int64_t(1) << 31) || nq_pad >= (int64_t(1) << 31)) return sg::fail(SG_ERR_ARG, "sg_knn: too many rows");
@@ -402,9 +344,9 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   nsplit = std::min(nsplit, 256);
   const int64_t rps = sg::ceil_div(sg::ceil_div(nr, nsplit), BN) * BN;
   nsplit = int(sg::ceil_div(nr, rps));
-  const bool same = (queries == refs) && (nq == nr);
+  const int fold = d <= BK - 3 ? 1 : 0;
   const size_t need = sg::Carver::need(size_t(nr_pad) * BK * 2) + sg::Carver::need(size_t(nr_pad) * 4) +
-                      (same ? 0 : sg::Carver::need(size_t(nq_pad) * BK * 2)) +
+                      sg::Carver::need(size_t(nq_pad) * BK * 2) +
                       sg::Carver::need(sizeof(int) * size_t(nsplit) * nq_pad * kc) + sg::Carver::need(sizeof(int));
   int status;
   void* w = sg::ws_get(h, need, &status);
@@ -412,27 +354,26 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   sg::Carver cv(w);
   __nv_bfloat16* Rb = cv.take<__nv_bfloat16>(size_t(nr_pad) * BK);
   float* rn = cv.take<float>(nr_pad);
-  __nv_bfloat16* Qb = same ? Rb : cv.take<__nv_bfloat16>(size_t(nq_pad) * BK);
+  __nv_bfloat16* Qb = cv.take<__nv_bfloat16>(size_t(nq_pad) * BK);
   int* cand = cv.take<int>(size_t(nsplit) * nq_pad * kc);
   int* err = cv.take<int>(1);
   SG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-  to_bf16_kernel<<<sg::ceil_div_i(nr_pad, 256), 256, 0, st>>>(refs, nr, d, ld, Rb, nr_pad, rn);
+  refs_bf16_kernel<<<sg::ceil_div_i(nr_pad, 256), 256, 0, st>>>(refs, nr, d, ld, fold, Rb, nr_pad, rn);
   SG_LAUNCH_CHECK();
-  if (!same) {
-    to_bf16_kernel<<<sg::ceil_div_i(nq_pad, 256), 256, 0, st>>>(queries, nq, d, ld, Qb, nq_pad, nullptr);
-    SG_LAUNCH_CHECK();
-  }
+  queries_bf16_kernel<<<sg::ceil_div_i(nq_pad, 256), 256, 0, st>>>(queries, nq, d, ld, fold, Qb, nq_pad);
+  SG_LAUNCH_CHECK();
   CUtensorMap ta, tb;
-  int rc = make_map(&ta, Qb, same ? nr_pad : nq_pad, BM);
+  int rc = make_map(&ta, Qb, nq_pad, BM);
   if (rc) return rc;
   rc = make_map(&tb, Rb, nr_pad, BN);
   if (rc) return rc;
   {
   sg::ProfScope prof(h, "knn_tc", st);
-  if (kc == 16) rc = launch_tc<16>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, err, st);
-  else if (kc == 32) rc = launch_tc<32>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, err, st);
-  else if (kc == 48) rc = launch_tc<48>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, err, st);
-  else rc = launch_tc<64>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, err, st);
+  if (kc == 16) rc = launch_tc<16>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, err, st);
+  else if (kc == 32) rc = launch_tc<32>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, err, st);
+  else if (kc == 40) rc = launch_tc<40>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, err, st);
+  else if (kc == 48) rc = launch_tc<48>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, err, st);
+  else rc = launch_tc<64>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, err, st);
   }
   if (rc) return rc;
   int herr = 0;

@@ -22,7 +22,7 @@ from . import kernels as K
 PLAIN_MARGIN = 0
 PRECISION_MARGIN = 16
 # covariance forms with a kernel in this build
-COV_FORMS = ("plain",)
+COV_FORMS = ("plain", "precision")
 
 
 @dataclass

@@ -122,6 +122,29 @@ def test_covariance_plain(K, counts):
     assert np.allclose(zs2.cpu().numpy(), zm.sum(0), atol=1e-2)
 
 
+def test_covariance_precision(K, counts):
+    # 3xBF16 split products on the tensor cores, FP32 accumulation, FP64 reduction
+    x, cs, cq, _ = _normalize(K, counts)
+    mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
+    xw, omu, osg, z = _zscaled(counts)
+    h = z.shape[1]
+    cov, zsum = K.covariance(x, mu32, sg32, n_cols=h, precision="precision")
+    torch.cuda.synchronize()
+    want = z.T @ z
+    got = cov.cpu().numpy()
+    assert np.abs(got - want).max() <= 1e-4 * np.abs(want).max()
+    assert np.array_equal(got, got.T)
+    assert np.abs(zsum.cpu().numpy() - z.sum(0)).max() < 1e-2
+    mask = (np.arange(x.shape[0]) % 3 != 0).astype(np.uint8)
+    cov2, _ = K.covariance(x, mu32, sg32, n_cols=h, row_mask=cu(mask), precision="precision")
+    zm = z[mask.astype(bool)]
+    assert np.abs(cov2.cpu().numpy() - zm.T @ zm).max() <= 1e-4 * np.abs(want).max()
+    # the leading principal axes agree with the FP64 oracle
+    comps, evals, _, _ = K.pca_basis(cov, zsum, x.shape[0], 11, n_load=10, ld_l=10)
+    ocomp, oev = oracle.pca_exact(z, 11)
+    assert oracle.subspace_angles(comps.cpu().numpy()[:, :5], ocomp[:, :5]).max() < 1e-3
+
+
 def test_pca_basis_and_projection(K, counts):
     x, cs, cq, _ = _normalize(K, counts)
     mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
