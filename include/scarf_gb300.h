@@ -155,6 +155,24 @@ int sg_smooth(sg_handle* h, const int64_t* knn_idx, const float* knn_dist, int64
               int32_t k, double local_connectivity, double bandwidth, int64_t chunk_rows,
               int64_t* edges_out, double* w_out, void* stream);
 
+/* sg_smooth for callers that must not have device memory allocated on their
+ * behalf (a host that owns the whole HBM budget through its own pool, a
+ * latency-critical loop that cannot take cudaMalloc's device-wide
+ * synchronisation, a plugin host that forbids allocations outside its
+ * allocator). No counterpart in the reference: scarf never touches a device.
+ * Same arguments and results as sg_smooth without a handle; runs on the
+ * current device. Its scratch is a fixed array of static device memory in the
+ * library (about 8.3 MB, held on every GPU that loads the library until the
+ * process exits): at most 2^21 edges (n*k) and 2^14 chunks per call, larger
+ * requests return SG_ERR_ARG. Nothing is allocated or freed. The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture. All calls share the one array,
+ * so calls whose work overlaps on the GPU (other streams, other host threads)
+ * race: order them. */
+int sg_smooth_noalloc(const int64_t* knn_idx, const float* knn_dist, int64_t n, int32_t k,
+                      double local_connectivity, double bandwidth, int64_t chunk_rows,
+                      int64_t* edges_out, double* w_out, void* stream);
+
 /* a9 -- fuzzy union of the graph G given as COO (edges[nnz*2] int64 pairs,
  * w[nnz] float64, k edges per row in row-major order; use_k < k keeps the first
  * use_k of each row as _store_to_sparse does, graph_datastore.py:474-511;

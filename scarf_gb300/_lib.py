@@ -54,6 +54,7 @@ SIGNATURES = {
     "sg_project": (C.c_int, [vp, vp, i64, i32, i64, vp, vp, vp, i32, i32, vp, i32, vp, i32, vp]),
     "sg_knn": (C.c_int, [vp, vp, i64, vp, i64, i32, i32, i32, i64, i32, i32, vp, vp, vp, vp]),
     "sg_smooth": (C.c_int, [vp, vp, vp, i64, i32, f64, f64, i64, vp, vp, vp]),
+    "sg_smooth_noalloc": (C.c_int, [vp, vp, i64, i32, f64, f64, i64, vp, vp, vp]),
     "sg_fuzzy_union": (C.c_int, [vp, vp, vp, i64, i64, i32, i32, f64, u32, vp, vp, vp, i64, vp]),
 }
 

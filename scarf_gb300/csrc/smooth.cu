@@ -13,6 +13,8 @@
 // A chunk-mean pre-pass supplies the floor of rows whose rho is 0.
 #include "common.cuh"
 
+#include <mutex>
+
 namespace {
 
 constexpr int kRowsPerCta = 128;
@@ -212,6 +214,90 @@ extern "C" int sg_smooth(sg_handle* h, const int64_t* knn_idx, const float* knn_
   const size_t smem = sizeof(float) * kRowsPerCta * (k + 1);
   SG_CUDA(cudaFuncSetAttribute(smooth_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   sg::ProfScope prof(h, "smooth", st);
+  smooth_kernel<<<sg::ceil_div_i(n, kRowsPerCta), kRowsPerCta, smem, st>>>(
+      knn_idx, knn_dist, n, k, local_connectivity, target, chunk_rows, csum, edges_out, w_out, w32, cmin,
+      czero);
+  SG_LAUNCH_CHECK();
+  global_min_kernel<<<1, 256, 0, st>>>(cmin, czero, nchunks, gmin);
+  SG_LAUNCH_CHECK();
+  fix_zeros_kernel<<<unsigned(nchunks), 256, 0, st>>>(w32, w_out, n, k, chunk_rows, czero, gmin);
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Smoothing without any device allocation.
+//
+// Some callers cannot let a library allocate device memory: a host that owns
+// the whole HBM budget through its own pool (a serving process sized to the
+// last byte), code that must not take cudaMalloc's implicit device-wide
+// synchronisation in a latency-critical loop, or a plugin host that forbids
+// allocations outside its allocator. For them, sg_smooth_noalloc does what
+// sg_smooth does with its scratch held in a fixed array that belongs to this
+// file (static device memory, reserved on every GPU that loads the library
+// until the process exits): at most kNoallocMaxEdges = 2^21 edges (n * k) and
+// kNoallocMaxChunks = 2^14 chunks per call, about 8.3 MB per GPU.
+namespace {
+
+constexpr int64_t kNoallocMaxEdges = int64_t(1) << 21;
+constexpr int64_t kNoallocMaxChunks = int64_t(1) << 14;
+constexpr size_t kNoallocW32 = sizeof(float) * size_t(kNoallocMaxEdges);
+constexpr size_t kNoallocSum = sizeof(double) * size_t(kNoallocMaxChunks);
+constexpr size_t kNoallocU32 = sizeof(unsigned) * size_t(kNoallocMaxChunks);
+constexpr size_t kNoallocBytes = kNoallocW32 + kNoallocSum + 2 * kNoallocU32 + 256;
+
+static __device__ __align__(256) unsigned char g_smooth_scratch[kNoallocBytes];
+
+// device address of g_smooth_scratch per device, looked up on first use
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {};
+
+}  // namespace
+
+extern "C" int sg_smooth_noalloc(const int64_t* knn_idx, const float* knn_dist, int64_t n, int32_t k,
+                                 double local_connectivity, double bandwidth, int64_t chunk_rows,
+                                 int64_t* edges_out, double* w_out, void* stream) {
+  sg::clear_error();
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  SG_ARG(knn_idx && knn_dist && edges_out && w_out, "sg_smooth_noalloc: null pointer argument");
+  SG_ARG(n >= 0 && k >= 1 && k <= kMaxK, "sg_smooth_noalloc: k=%d outside [1, %d]", k, kMaxK);
+  SG_ARG(chunk_rows >= 1, "sg_smooth_noalloc: chunk_rows must be >= 1");
+  if (n == 0) return SG_OK;
+  const int64_t nchunks = sg::ceil_div(n, chunk_rows);
+  SG_ARG(n * k <= kNoallocMaxEdges,
+         "sg_smooth_noalloc: %lld edges (n*k) exceed the fixed scratch limit of %lld; use sg_smooth",
+         (long long)(n * k), (long long)kNoallocMaxEdges);
+  SG_ARG(nchunks <= kNoallocMaxChunks,
+         "sg_smooth_noalloc: %lld chunks exceed the fixed scratch limit of %lld; use larger chunk_rows or sg_smooth",
+         (long long)nchunks, (long long)kNoallocMaxChunks);
+  int dev = 0;
+  SG_CUDA(cudaGetDevice(&dev));
+  SG_ARG(dev >= 0 && dev < 64, "sg_smooth_noalloc: device ordinal %d not supported", dev);
+  char* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* p = nullptr;
+      SG_CUDA(cudaGetSymbolAddress(&p, g_smooth_scratch));
+      g_noalloc_addr[dev] = p;
+    }
+    base = static_cast<char*>(g_noalloc_addr[dev]);
+  }
+  float* w32 = reinterpret_cast<float*>(base);
+  double* csum = reinterpret_cast<double*>(base + kNoallocW32);
+  unsigned* cmin = reinterpret_cast<unsigned*>(base + kNoallocW32 + kNoallocSum);
+  int* czero = reinterpret_cast<int*>(base + kNoallocW32 + kNoallocSum + kNoallocU32);
+  float* gmin = reinterpret_cast<float*>(base + kNoallocW32 + kNoallocSum + 2 * kNoallocU32);
+  // the previous call's contents stay in the array: every piece read below is
+  // first written in this call (chunk flags and minima by init_chunks_kernel,
+  // chunk sums, float weights and the global minimum by their kernels)
+  init_chunks_kernel<<<sg::ceil_div_i(nchunks, 256), 256, 0, st>>>(cmin, czero, nchunks);
+  SG_LAUNCH_CHECK();
+  chunk_sum_kernel<<<unsigned(nchunks), 256, 0, st>>>(knn_dist, n, k, chunk_rows, csum);
+  SG_LAUNCH_CHECK();
+  const double target = log2(double(k)) * bandwidth;
+  const size_t smem = sizeof(float) * kRowsPerCta * (k + 1);
+  SG_CUDA(cudaFuncSetAttribute(smooth_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   smooth_kernel<<<sg::ceil_div_i(n, kRowsPerCta), kRowsPerCta, smem, st>>>(
       knn_idx, knn_dist, n, k, local_connectivity, target, chunk_rows, csum, edges_out, w_out, w32, cmin,
       czero);
