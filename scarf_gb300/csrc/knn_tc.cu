@@ -16,6 +16,8 @@
 // The candidates are re-ranked exactly in FP32 by knn.cu.
 #include "tc_ptx.cuh"
 
+#include <type_traits>
+
 #include <algorithm>
 
 int sg_rerank(const float* queries, const float* refs, int d, int ld, int64_t nq, const int* cand, int nlists, int kc,
@@ -196,17 +198,21 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       cnt = 0;
       thr = top.worst();
     };
-    // filter one chunk of 32 accumulator columns into the buffer
-    auto process = [&](const uint32_t (&r)[32], int ch, int64_t r0, bool use_rn, int lim) {
+    // filter one chunk of 32 accumulator columns into the buffer; kRn: add
+    // |r|^2 here (not folded into the MMA); kMask: last tile, columns >= lim
+    // are past the last reference
+    auto process = [&](auto rn_tag, auto mask_tag, const uint32_t (&r)[32], int ch, int64_t r0, int lim) {
+      constexpr bool kRn = decltype(rn_tag)::value;
+      constexpr bool kMask = decltype(mask_tag)::value;
       const int cbase = int(r0) + ch * 32;
 #pragma unroll
       for (int j = 0; j < 32; j += 8) {
         float kk[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          const float a = __uint_as_float(r[j + q]);
-          float key = use_rn ? fmaf(-2.f, a, my_rn[ch * 32 + j + q]) : a;
-          if (lim < BN && ch * 32 + j + q >= lim) key = __int_as_float(0x7f800000);
+          float key = __uint_as_float(r[j + q]);
+          if (kRn) key = fmaf(-2.f, key, my_rn[ch * 32 + j + q]);
+          if (kMask && ch * 32 + j + q >= lim) key = __int_as_float(0x7f800000);
           kk[q] = key;
         }
         const float m = fminf(fminf(fminf(kk[0], kk[1]), fminf(kk[2], kk[3])),
@@ -221,6 +227,16 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
             }
           }
         }
+      }
+    };
+    auto filter = [&](const uint32_t (&r)[32], int ch, int64_t r0, int lim) {
+      using T = std::true_type;
+      using F = std::false_type;
+      if (fold) {
+        if (lim < BN) process(F{}, T{}, r, ch, r0, lim);
+        else process(F{}, F{}, r, ch, r0, lim);
+      } else {
+        process(T{}, F{}, r, ch, r0, lim);  // padding references carry |r|^2 = +inf
       }
     };
     for (int t = 0; t < ntiles; ++t) {
@@ -247,11 +263,11 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       for (int ch = 0; ch < BN / 32; ch += 2) {
         tmem_ld32(tbase + uint32_t((ch + 1) * 32), rb);
         if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
-        process(ra, ch, r0, use_rn, lim);
+        filter(ra, ch, r0, lim);
         tmem_wait_ld(rb);
         if (ch + 2 < BN / 32) tmem_ld32(tbase + uint32_t((ch + 2) * 32), ra);
         if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
-        process(rb, ch + 1, r0, use_rn, lim);
+        filter(rb, ch + 1, r0, lim);
         if (ch + 2 < BN / 32) tmem_wait_ld(ra);
       }
       tc_fence_before();

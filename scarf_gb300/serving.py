@@ -1,0 +1,293 @@
+"""Continuous-batching mapping service over a device-resident reference.
+
+The service answers the query of ``run_mapping``
+(scarf/datastore/mapping_datastore.py:198-208): normalise target cells onto
+the reference features (missing features filled with 1.0,
+scarf/mapping_utils.py:208), z-scale with the reference's mu/sigma, project
+with its loadings, and return the k nearest reference cells.
+
+Scheduling (``BatchScheduler``, pure host logic):
+* requests are admitted in arrival order while the HBM they need (their CSR,
+  normalised rows, scores and results) fits the budget; a request that cannot
+  fit the budget alone is rejected with ``MemoryError``;
+* each GPU batch takes up to ``max_batch_rows`` rows from the admitted
+  requests, oldest first, so a large request is processed in row slices and
+  requests that arrive while it is on the GPU join the next batches instead of
+  waiting for it to finish;
+* a request completes when all its rows are back; its memory is released and
+  the next queued requests are admitted.
+
+Execution (``MappingServer``): ``n_workers`` host threads, each with its own
+CUDA stream and library handle, take batches from the scheduler; the copies
+and kernels of different batches overlap on the device. Rows are independent,
+so a request's result does not depend on what it was batched with.
+"""
+from __future__ import annotations
+
+import collections
+import threading
+import time
+from dataclasses import dataclass, field
+from typing import Deque, List, Optional, Tuple
+
+import numpy as np
+
+
+@dataclass
+class MapRequest:
+    rid: int
+    indptr: np.ndarray
+    indices: np.ndarray
+    data: np.ndarray
+    k: int
+    arrival: float
+    n_cells: int = 0
+    bytes_needed: int = 0
+    next_row: int = 0
+    rows_done: int = 0
+    idx: Optional[np.ndarray] = None
+    dist: Optional[np.ndarray] = None
+    t_done: Optional[float] = None
+    error: Optional[BaseException] = None
+    done: threading.Event = field(default_factory=threading.Event)
+
+    def __post_init__(self):
+        self.n_cells = len(self.indptr) - 1
+
+    @property
+    def latency_ms(self) -> Optional[float]:
+        return None if self.t_done is None else (self.t_done - self.arrival) * 1e3
+
+    def result(self, timeout: Optional[float] = None):
+        if not self.done.wait(timeout):
+            raise TimeoutError(f"request {self.rid} not done")
+        if self.error is not None:
+            raise self.error
+        return self.idx, self.dist
+
+
+Slice = Tuple[MapRequest, int, int]
+
+
+class BatchScheduler:
+    """HBM-budget admission and row-sliced continuous batching (host only)."""
+
+    def __init__(self, hbm_budget_bytes: int, max_batch_rows: int, bytes_per_row: int, bytes_per_nnz: int = 8):
+        self.budget = int(hbm_budget_bytes)
+        self.max_rows = int(max_batch_rows)
+        self.bytes_per_row = int(bytes_per_row)
+        self.bytes_per_nnz = int(bytes_per_nnz)
+        self.queued: Deque[MapRequest] = collections.deque()
+        self.active: List[MapRequest] = []
+        self.in_use = 0
+        self.lock = threading.Condition()
+        self.closed = False
+
+    def cost(self, req: MapRequest) -> int:
+        return req.n_cells * self.bytes_per_row + int(req.indptr[-1] - req.indptr[0]) * self.bytes_per_nnz
+
+    def submit(self, req: MapRequest) -> MapRequest:
+        req.bytes_needed = self.cost(req)
+        with self.lock:
+            if req.bytes_needed > self.budget:
+                req.error = MemoryError(f"request {req.rid} needs {req.bytes_needed} bytes of HBM, more than the "
+                                        f"budget of {self.budget}")
+                req.t_done = time.perf_counter()
+                req.done.set()
+                return req
+            if req.n_cells == 0:
+                req.idx = np.zeros((0, req.k), np.int64)
+                req.dist = np.zeros((0, req.k), np.float32)
+                req.t_done = time.perf_counter()
+                req.done.set()
+                return req
+            self.queued.append(req)
+            self._admit()
+            self.lock.notify_all()
+        return req
+
+    def _admit(self):
+        while self.queued and self.in_use + self.queued[0].bytes_needed <= self.budget:
+            r = self.queued.popleft()
+            self.in_use += r.bytes_needed
+            r.idx = np.empty((r.n_cells, r.k), np.int64)
+            r.dist = np.empty((r.n_cells, r.k), np.float32)
+            self.active.append(r)
+
+    def next_batch(self, timeout: Optional[float] = None) -> List[Slice]:
+        """Up to max_rows rows from the admitted requests, oldest first."""
+        with self.lock:
+            end = None if timeout is None else time.perf_counter() + timeout
+            while not self.closed and not any(r.next_row < r.n_cells for r in self.active):
+                left = None if end is None else end - time.perf_counter()
+                if left is not None and left <= 0:
+                    return []
+                self.lock.wait(left)
+            batch: List[Slice] = []
+            room = self.max_rows
+            for r in self.active:
+                if room == 0:
+                    break
+                if r.next_row >= r.n_cells:
+                    continue
+                take = min(room, r.n_cells - r.next_row)
+                batch.append((r, r.next_row, r.next_row + take))
+                r.next_row += take
+                room -= take
+            return batch
+
+    def complete(self, batch: List[Slice], idx: np.ndarray, dist: np.ndarray, error: Optional[BaseException] = None):
+        """Scatter a finished batch back into its requests."""
+        now = time.perf_counter()
+        with self.lock:
+            off = 0
+            for r, a, b in batch:
+                n = b - a
+                if error is None:
+                    r.idx[a:b] = idx[off:off + n]
+                    r.dist[a:b] = dist[off:off + n]
+                else:
+                    r.error = error
+                off += n
+                r.rows_done += n
+                if r.rows_done == r.n_cells or error is not None:
+                    if r in self.active:
+                        self.active.remove(r)
+                        self.in_use -= r.bytes_needed
+                    r.t_done = now
+                    r.done.set()
+            self._admit()
+            self.lock.notify_all()
+
+    def close(self):
+        with self.lock:
+            self.closed = True
+            self.lock.notify_all()
+
+
+class MappingServer:
+    """GPU executor of the scheduler's batches (see the module docstring).
+
+    ``reference`` is an ``AnnStream`` (device-resident scores, mu/sigma,
+    loadings); ``target_gene_ids`` is the gene panel of the queries, aligned
+    once to the reference features."""
+
+    def __init__(self, reference, ref_feature_ids, target_gene_ids, k: int = 11, max_batch_rows: int = 16384,
+                 hbm_budget_bytes: int = 8 << 30, n_workers: int = 2, size_factor: float = 1000.0,
+                 log_transform: bool = True, renormalize_subset: bool = True, precision: Optional[str] = None):
+        import torch
+
+        from .datastore import align_col_map
+        self.ref = reference
+        self.k = int(k)
+        self.size_factor = float(size_factor)
+        self.log_transform = log_transform
+        self.renorm = renormalize_subset
+        self.precision = precision or reference.annIdx.precision
+        self.device = reference.data.x.device
+        cmap, missing = align_col_map(np.asarray(ref_feature_ids), np.asarray(target_gene_ids))
+        self.cmap = torch.from_numpy(cmap).to(self.device)
+        self.missing = torch.from_numpy(missing).to(self.device)
+        h = reference.nFeats
+        ld = (h + 3) // 4 * 4
+        lds = (reference.dims + 3) // 4 * 4
+        per_row = 8 + ld * 4 + lds * 4 + self.k * 12
+        self.sched = BatchScheduler(hbm_budget_bytes, max_batch_rows, per_row)
+        self.n_workers = int(n_workers)
+        self._threads: List[threading.Thread] = []
+        self._rid = 0
+        self._rid_lock = threading.Lock()
+        self.batches_run = 0
+
+    # -- client side ----------------------------------------------------------
+    def submit(self, indptr, indices, data, arrival: Optional[float] = None) -> MapRequest:
+        with self._rid_lock:
+            rid = self._rid
+            self._rid += 1
+        req = MapRequest(rid, np.asarray(indptr, np.int64), np.asarray(indices, np.int32), np.asarray(data, np.int32),
+                         self.k, arrival if arrival is not None else time.perf_counter())
+        return self.sched.submit(req)
+
+    def start(self):
+        for i in range(self.n_workers):
+            t = threading.Thread(target=self._worker, name=f"sg-map-{i}", daemon=True)
+            t.start()
+            self._threads.append(t)
+        return self
+
+    def stop(self):
+        self.sched.close()
+        for t in self._threads:
+            t.join(timeout=30)
+        self._threads = []
+
+    def __enter__(self):
+        return self.start()
+
+    def __exit__(self, *exc):
+        self.stop()
+
+    # -- worker side ----------------------------------------------------------
+    def _worker(self):
+        import torch
+
+        from . import kernels as K
+        torch.cuda.set_device(self.device)
+        stream = torch.cuda.Stream(self.device)
+        ref = self.ref
+        h = ref.nFeats
+        while True:
+            batch = self.sched.next_batch(timeout=0.05)
+            if not batch:
+                if self.sched.closed:
+                    return
+                continue
+            try:
+                ip, ind, dat = _concat_rows(batch)
+                with torch.cuda.stream(stream):
+                    t_ip = torch.from_numpy(ip).pin_memory().to(self.device, non_blocking=True)
+                    t_ind = torch.from_numpy(ind).pin_memory().to(self.device, non_blocking=True)
+                    t_dat = torch.from_numpy(dat).pin_memory().to(self.device, non_blocking=True)
+                    x = K.normalize_csr(t_ip, t_ind, t_dat, self.cmap, h, size_factor=self.size_factor,
+                                        log_transform=self.log_transform, renormalize_subset=self.renorm,
+                                        missing_mask=self.missing, fill_value=1.0)
+                    s = K.project(x, ref._mu32, ref._sg32, ref._l32, ref.dims, n_cols=h)
+                    idx, dist, _ = K.knn(s, ref.annIdx.scores, ref.dims, self.k, self_offset=-1,
+                                         margin=ref.annIdx._margin(), precision=self.precision)
+                    hi = torch.empty(idx.shape, dtype=idx.dtype, pin_memory=True)
+                    hd = torch.empty(dist.shape, dtype=dist.dtype, pin_memory=True)
+                    hi.copy_(idx, non_blocking=True)
+                    hd.copy_(dist, non_blocking=True)
+                stream.synchronize()
+                self.batches_run += 1
+                self.sched.complete(batch, hi.numpy(), hd.numpy())
+            except BaseException as e:  # surfaces in MapRequest.result()
+                self.sched.complete(batch, None, None, error=e)
+
+
+def _concat_rows(batch: List[Slice]):
+    """One CSR of the batch's row slices (indptr rebased to 0)."""
+    ptrs, inds, dats = [np.zeros(1, np.int64)], [], []
+    base = 0
+    for r, a, b in batch:
+        p0, p1 = int(r.indptr[a]), int(r.indptr[b])
+        seg = r.indptr[a + 1:b + 1] - p0 + base
+        ptrs.append(seg.astype(np.int64))
+        inds.append(r.indices[p0:p1])
+        dats.append(r.data[p0:p1])
+        base += p1 - p0
+    ind = np.concatenate(inds) if inds else np.zeros(0, np.int32)
+    dat = np.concatenate(dats) if dats else np.zeros(0, np.int32)
+    if ind.size == 0:  # keep the device pointers valid for an all-empty batch
+        ind = np.zeros(1, np.int32)
+        dat = np.zeros(1, np.int32)
+    return np.concatenate(ptrs), ind, dat
+
+
+def latency_summary(requests: List[MapRequest]) -> dict:
+    lat = np.array([r.latency_ms for r in requests if r.latency_ms is not None and r.error is None])
+    cells = sum(r.n_cells for r in requests if r.error is None)
+    if lat.size == 0:
+        return {"requests": 0}
+    return {"requests": int(lat.size), "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "max_ms": float(lat.max()), "cells": int(cells)}
