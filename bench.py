@@ -283,6 +283,7 @@ def run_gb300(args, cfg):
     K.profile(False)
     if c_u:
         prof_ms["union"] = (t_u / c_u, 0.0)
+    eig = eigensolver_comparison(K, pipeline, ip_d, ind_d, dat_d, G, feat, n, dims)
     pk = peaks()
     work = kernel_work(cfg, csr.nnz)
     kernels = {}
@@ -326,8 +327,8 @@ def run_gb300(args, cfg):
         "vs_baseline": None,
         "dtype": "bf16",
         "data": "synthetic (seeded negative-binomial counts generated on the device)",
-        "config": {"workload": cfg["name"], "form": "precision: bf16 tcgen05 distances, f32 re-rank, "
-                   "f32 normalise/scatter/projection, f64 eigh", "margin": 16, "batch_size": BATCH,
+        "config": {"workload": cfg["name"], "form": "precision: 3xbf16 tcgen05 scatter, f32 partial eigh + f64 "
+                   "Rayleigh-Ritz, bf16 tcgen05 distances, f32 re-rank", "margin": 16, "batch_size": BATCH,
                    "nnz": csr.nnz, "l2": "inputs larger than L2 (CSR %.2f GB, normalised matrix %.2f GB)"
                    % (h2d / 1e9, n * cfg["n_hvg"] * 4 / 1e9), "parallelism": f"replicas x{ws}"},
         "recall_at_k": round(rec, 5),
@@ -337,6 +338,7 @@ def run_gb300(args, cfg):
                   "same_neighbour_frac": round(same_nbr, 5), "max_weight_diff": w_diff,
                   "kernels_ms": {k_: round(v[0], 4) for k_, v in prof_p.items()}},
         "kernels": kernels,
+        "eigensolver": eig,
         "e2e": {"value": round(cells / (e2e_ms * 1e-3), 1), "unit": "cells/s", "ms_per_step": round(e2e_ms, 3),
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": roof,
@@ -349,6 +351,41 @@ def run_gb300(args, cfg):
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+def eigensolver_comparison(K, pipeline, ip, ind, dat, G, feat, n, dims, reps=3):
+    """FP64 partial eigendecomposition (the default) against the mixed FP32 +
+    FP64 Rayleigh-Ritz solver on this workload's scatter: device time of each
+    and the principal angles between their leading subspaces."""
+    import torch
+    x, cs, cq = pipeline.normalize_csr_host(ip, ind, dat, G, feat, device=ip.device)
+    mu, sg, mu32, sg32 = K.zstats(cs, cq, n)
+    cov, zsum = K.covariance(x, mu32, sg32, n_cols=len(feat), precision="precision")
+    del x
+    out = {}
+    comps = {}
+    for method in ("fp64", "mixed"):
+        K.pca_basis(cov, zsum, n, dims + 1, n_load=dims, ld_l=dims, eigh=method)
+        torch.cuda.synchronize()
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            c, ev, _, _ = K.pca_basis(cov, zsum, n, dims + 1, n_load=dims, ld_l=dims, eigh=method)
+        e1.record(st)
+        torch.cuda.synchronize()
+        out[f"{method}_ms"] = round(e0.elapsed_time(e1) / reps, 3)
+        comps[method] = (c.cpu().numpy(), ev.cpu().numpy())
+
+    def angle(a, b):
+        qa, _ = np.linalg.qr(a)
+        qb, _ = np.linalg.qr(b)
+        return float(np.arccos(np.clip(np.linalg.svd(qa.T @ qb, compute_uv=False), -1, 1)).max())
+    a, b = comps["fp64"][0], comps["mixed"][0]
+    out["max_angle_top10_rad"] = angle(a[:, :10], b[:, :10])
+    out["max_angle_all_rad"] = angle(a[:, :dims], b[:, :dims])
+    out["max_eval_rel_diff"] = float(np.max(np.abs(comps["fp64"][1] - comps["mixed"][1]) / np.abs(comps["fp64"][1])))
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -442,8 +479,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--mode", default="full", choices=["full", "step"],
-                    help="step: warm-up steps then one make_graph step and nothing else (for profilers)")
+    ap.add_argument("--mode", default="full", choices=["full", "step", "serve"],
+                    help="step: warm-up steps then one make_graph step and nothing else (for profilers); "
+                         "serve: the mapping service's latency under a Poisson request stream")
     ap.add_argument("--form", default="precision", choices=["precision", "plain"], help="form used by --mode step")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "gb300" else args.warmup
@@ -452,8 +490,94 @@ def main():
         run_reference(args, cfg)
     elif args.mode == "step":
         run_step(args, cfg)
+    elif args.mode == "serve":
+        run_serve(args)
     else:
         run_gb300(args, cfg)
+
+
+SERVE = dict(name="C4: mapping service over a device-resident 500,000-cell reference (30,000 genes NB, 20 clusters, "
+                   "2,000 HVGs, 50 PCs, BF16 projection); Poisson stream of query batches of log-uniform "
+                   "100-50,000 cells drawn from the same populations with library sizes shifted to 2,200 UMIs; k=11",
+             n_ref=500_000, n_genes=30_000, n_clusters=20, n_hvg=2000, dims=50, k=11, lib_median=3000.0,
+             query_lib=2200.0, pool=60_000, n_requests=120, rate_hz=40.0, max_batch_rows=16384)
+
+
+def run_serve(args):
+    """p50/p99 request latency and cells/s of the continuous-batching mapper."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from scarf_gb300 import pipeline, synth
+    from scarf_gb300.serving import MappingServer, Reference, latency_summary
+    c = SERVE
+    dev = torch.device("cuda", 0)
+    ref_csr = synth.nb_counts(c["n_ref"], c["n_genes"], c["n_clusters"], SEED, lib_median=c["lib_median"],
+                              device=dev)
+    feat = synth.select_hvgs(ref_csr, c["n_hvg"])
+    ip, ind, dat = (torch.from_numpy(a).to(dev) for a in (ref_csr.indptr, ref_csr.indices, ref_csr.data))
+    g = pipeline.make_graph(ip, ind, dat, ref_csr.n_genes, feat, c["dims"], c["k"], precision="precision",
+                            smooth=False, keep_x=False)
+    del ip, ind, dat
+    ref = Reference.from_graph(g, precision="precision")
+    pool = synth.nb_counts(c["pool"], c["n_genes"], c["n_clusters"], SEED, lib_median=c["query_lib"], device=dev,
+                           cells_seed=SEED + 1)
+    rng = np.random.default_rng(7)
+    sizes = np.exp(rng.uniform(np.log(100), np.log(50_000), c["n_requests"])).astype(int)
+    gaps = rng.exponential(1.0 / c["rate_hz"], c["n_requests"])
+    starts = [int(rng.integers(0, c["pool"] - s + 1)) for s in sizes]
+    genes = np.arange(c["n_genes"]).astype(str)
+
+    def slice_rows(a, n):
+        p0, p1 = int(pool.indptr[a]), int(pool.indptr[a + n])
+        return pool.indptr[a:a + n + 1] - p0, pool.indices[p0:p1], pool.data[p0:p1]
+
+    with MappingServer(ref, genes[feat], genes, k=c["k"], max_batch_rows=c["max_batch_rows"], n_workers=2,
+                       hbm_budget_bytes=16 << 30) as srv:
+        for s in (100, 5000, 20000):          # warm-up: handles, scratch, pinned staging
+            srv.submit(*slice_rows(0, s)).result(timeout=120)
+        reqs = []
+        t0 = time.perf_counter()
+        t = t0
+        for s, a, gap in zip(sizes, starts, gaps):
+            t += gap
+            now = time.perf_counter()
+            if t > now:
+                time.sleep(t - now)
+            reqs.append(srv.submit(*slice_rows(a, int(s)), arrival=t))
+        for r in reqs:
+            r.result(timeout=600)
+        t_end = max(r.t_done for r in reqs)
+        batches = srv.batches_run
+    summ = latency_summary(reqs)
+    small = latency_summary([r for r in reqs if r.n_cells <= 10_000])
+    # recall of one mid-size request against exact FP64 kNN on the device
+    r = reqs[int(np.argsort(sizes)[len(sizes) // 2])]
+    qi = r.idx
+    a = starts[reqs.index(r)]
+    from scarf_gb300 import kernels as K
+    from scarf_gb300.datastore import align_col_map
+    cmap, missing = align_col_map(genes[feat], genes)
+    qp, qind, qdat = slice_rows(a, r.n_cells)
+    x = K.normalize_csr(torch.from_numpy(qp).to(dev), torch.from_numpy(qind).to(dev), torch.from_numpy(qdat).to(dev),
+                        torch.from_numpy(cmap).to(dev), len(feat), missing_mask=torch.from_numpy(missing).to(dev))
+    qs = K.project(x, g.mu32, g.sigma32, g.loadings32.contiguous(), g.dims, n_cols=len(feat))[:, :g.dims].double()
+    rs = g.scores[:, :g.dims].double()
+    d2 = (qs * qs).sum(1, keepdim=True) + (rs * rs).sum(1)[None, :] - 2.0 * qs @ rs.T
+    kth = torch.topk(d2, c["k"], dim=1, largest=False).values[:, -1]
+    got = torch.from_numpy(qi).to(dev)
+    dg = ((qs[:, None, :] - rs[got]) ** 2).sum(-1)
+    rec = float((dg <= kth[:, None] * (1 + 1e-6) + 1e-12).double().mean().item())
+    print(json.dumps({
+        "metric": "mapping latency p99 (ms)", "value": round(summ["p99_ms"], 3), "unit": "ms",
+        "higher_is_better": False, "p50_ms": round(summ["p50_ms"], 3), "p99_ms": round(summ["p99_ms"], 3),
+        "p99_ms_requests_le_10k_cells": round(small.get("p99_ms", float("nan")), 3),
+        "p50_ms_requests_le_10k_cells": round(small.get("p50_ms", float("nan")), 3),
+        "requests": summ["requests"], "cells": summ["cells"],
+        "cells_per_s": round(summ["cells"] / (t_end - t0), 1), "gpu_batches": batches,
+        "recall_at_k_sampled_request": round(rec, 5), "data": "synthetic",
+        "config": {"workload": c["name"], "arrival_rate_hz": c["rate_hz"], "max_batch_rows": c["max_batch_rows"],
+                   "workers": 2, "form": "precision"}}), flush=True)
 
 
 def run_step(args, cfg):

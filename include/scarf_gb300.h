@@ -117,6 +117,17 @@ int sg_pca_basis(sg_handle* h, const double* cov, const double* zsum, int64_t n_
                  int32_t n_cols, int32_t n_comp, double* comps, double* evals, double* evr,
                  int32_t n_load, float* loadings32, int32_t ld_l, void* stream);
 
+/* a4 -- the same outputs as sg_pca_basis from a mixed-precision solver: an
+ * FP32 partial eigendecomposition of the centred scatter (the n_comp + 16
+ * largest pairs), then an FP64 Rayleigh-Ritz step on that subspace (FP64
+ * Cholesky-QR, FP64 Q^T A Q and its FP64 eigendecomposition). Separated
+ * components agree with sg_pca_basis to FP32 eigenvector accuracy.
+ * Synchronises the stream. No counterpart in the reference beyond the
+ * IncrementalPCA fit it also replaces (scarf/ann.py:207-256). */
+int sg_pca_basis_mixed(sg_handle* h, const double* cov, const double* zsum, int64_t n_used,
+                       int32_t n_cols, int32_t n_comp, double* comps, double* evals, double* evr,
+                       int32_t n_load, float* loadings32, int32_t ld_l, void* stream);
+
 /* a5 -- the reducer ((x - mu)/sigma) . L (scarf/ann.py:129-138, :191-192):
  * scores[r*ld_s + c], c < d (columns d..ld_s-1 are written 0). bf16_out (may be
  * NULL) receives a BF16 copy with row stride ld_b (zero padded). */

@@ -75,7 +75,7 @@ def build(force: bool = False, verbose_ptx: bool = False, quiet: bool = True) ->
     objs = [str(o) for o, _ in logs]
     tmp = OUT / "libscarfgpu.so.tmp"
     cmd = [nvcc(), "-shared", "-o", str(tmp)] + objs + ARCH + [
-        "-L", cuda_lib_dir(), "-lcusolver", "-lcudart", "-Xlinker", "-rpath=" + cuda_lib_dir()]
+        "-L", cuda_lib_dir(), "-lcusolver", "-lcublas", "-lcudart", "-Xlinker", "-rpath=" + cuda_lib_dir()]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -18,6 +18,7 @@ struct sg_handle {
   void* ws = nullptr;        // scratch arena, grown on demand
   size_t ws_bytes = 0;
   void* solver = nullptr;    // cusolverDnHandle_t, created on first use
+  void* blas = nullptr;      // cublasHandle_t, created on first use
   void* solver_work = nullptr;
   size_t solver_work_bytes = 0;
   // kernel timing (off unless sg_profile(h, 1)): events around named launches

@@ -14,11 +14,13 @@ namespace {
 
 constexpr int kRounds = 8;  // rows per warp per CTA
 
-template <bool kBf16>
+// CM: element type of the gene -> column map (int16_t when the output has
+// fewer than 32768 columns, so that the map stays resident in L1)
+template <bool kBf16, typename CM>
 __global__ void normalize_kernel(const int64_t* __restrict__ indptr,
                                  const int32_t* __restrict__ indices,
                                  const int32_t* __restrict__ data, int64_t n_rows,
-                                 const int32_t* __restrict__ col_map, int64_t n_genes, int n_cols,
+                                 const CM* __restrict__ col_map, int64_t n_genes, int n_cols, int vec,
                                  int pitch, const uint8_t* __restrict__ missing, float fill,
                                  const double* __restrict__ n_counts, float sf, unsigned flags,
                                  void* __restrict__ out, int64_t ld_out,
@@ -50,25 +52,43 @@ __global__ void normalize_kernel(const int64_t* __restrict__ indptr,
     long long s = 0;
     if (valid) {
       const int64_t p0 = indptr[r] - base, p1 = indptr[r + 1] - base;
-      int64_t p = p0 + lane;
-      // four independent loads in flight per lane
-      for (; p + 96 < p1; p += 128) {
-        int g0 = indices[p], g1 = indices[p + 32], g2 = indices[p + 64], g3 = indices[p + 96];
-        int c0 = data[p], c1 = data[p + 32], c2 = data[p + 64], c3 = data[p + 96];
-        int m0 = (unsigned)g0 < (unsigned long long)n_genes ? col_map[g0] : -1;
-        int m1 = (unsigned)g1 < (unsigned long long)n_genes ? col_map[g1] : -1;
-        int m2 = (unsigned)g2 < (unsigned long long)n_genes ? col_map[g2] : -1;
-        int m3 = (unsigned)g3 < (unsigned long long)n_genes ? col_map[g3] : -1;
-        if ((unsigned)m0 < (unsigned)n_cols) { s += c0; atomicAdd(&row[m0], float(c0)); }
-        if ((unsigned)m1 < (unsigned)n_cols) { s += c1; atomicAdd(&row[m1], float(c1)); }
-        if ((unsigned)m2 < (unsigned)n_cols) { s += c2; atomicAdd(&row[m2], float(c2)); }
-        if ((unsigned)m3 < (unsigned)n_cols) { s += c3; atomicAdd(&row[m3], float(c3)); }
-      }
-      for (; p < p1; p += 32) {
-        int g = indices[p];
-        int c = data[p];
-        int m = (unsigned)g < (unsigned long long)n_genes ? col_map[g] : -1;
-        if ((unsigned)m < (unsigned)n_cols) { s += c; atomicAdd(&row[m], float(c)); }
+      auto take = [&](int g, int c) {
+        const int m = (unsigned)g < (unsigned long long)n_genes ? int(col_map[g]) : -1;
+        if ((unsigned)m < (unsigned)n_cols) {
+          s += c;
+          atomicAdd(&row[m], float(c));
+        }
+      };
+      if (vec) {
+        // up to 3 entries before the first 16-byte boundary, then 16-byte
+        // loads of indices and counts (two pairs in flight per lane), then
+        // each lane's partial last block
+        const int mis = int((reinterpret_cast<uintptr_t>(indices + p0) & 15) >> 2);
+        const int64_t pa = min(p1, p0 + ((4 - mis) & 3));
+        if (p0 + lane < pa) take(indices[p0 + lane], data[p0 + lane]);
+        int64_t q = pa + 4 * lane;
+        for (; q + 131 < p1; q += 256) {
+          const int4 g0 = *reinterpret_cast<const int4*>(indices + q);
+          const int4 c0 = *reinterpret_cast<const int4*>(data + q);
+          const int4 g1 = *reinterpret_cast<const int4*>(indices + q + 128);
+          const int4 c1 = *reinterpret_cast<const int4*>(data + q + 128);
+          take(g0.x, c0.x); take(g0.y, c0.y); take(g0.z, c0.z); take(g0.w, c0.w);
+          take(g1.x, c1.x); take(g1.y, c1.y); take(g1.z, c1.z); take(g1.w, c1.w);
+        }
+        for (; q + 3 < p1; q += 128) {
+          const int4 g0 = *reinterpret_cast<const int4*>(indices + q);
+          const int4 c0 = *reinterpret_cast<const int4*>(data + q);
+          take(g0.x, c0.x); take(g0.y, c0.y); take(g0.z, c0.z); take(g0.w, c0.w);
+        }
+        for (int64_t e = q; e < p1 && e < q + 4; ++e) take(indices[e], data[e]);
+      } else {
+        int64_t p = p0 + lane;
+        for (; p + 96 < p1; p += 128) {
+          const int g0 = indices[p], g1 = indices[p + 32], g2 = indices[p + 64], g3 = indices[p + 96];
+          const int c0 = data[p], c1 = data[p + 32], c2 = data[p + 64], c3 = data[p + 96];
+          take(g0, c0); take(g1, c1); take(g2, c2); take(g3, c3);
+        }
+        for (; p < p1; p += 32) take(indices[p], data[p]);
       }
     }
     s = warp_sum_ll(s);
@@ -175,6 +195,11 @@ __device__ __forceinline__ double clean_value(double v, double fill) {
   return v;
 }
 
+__global__ void narrow_map_kernel(const int32_t* __restrict__ in, int64_t n, int n_cols, int16_t* __restrict__ out) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = int16_t((in[i] < 0 || in[i] >= n_cols) ? -1 : in[i]);
+}
+
 __global__ void zstats_kernel(const double* __restrict__ colsum, const double* __restrict__ colsumsq,
                               double n, int n_cols, double* __restrict__ mu, double* __restrict__ sigma,
                               float* __restrict__ mu32, float* __restrict__ sigma32) {
@@ -228,39 +253,54 @@ extern "C" int sg_normalize_csr(sg_handle* h, const int64_t* indptr, const int32
   const int64_t rows_per_cta = int64_t(nwarps) * kRounds;
   const int nblocks = sg::ceil_div_i(n_rows, rows_per_cta);
 
+  const bool narrow = n_cols < 32768;
   float* ps = nullptr;
   float* pq = nullptr;
   double* gs = nullptr;
   double* gq = nullptr;
+  int16_t* map16 = nullptr;
   int ngroups = 0, per = 0;
-  if (colsum) {
+  {
     per = 32;
-    ngroups = sg::ceil_div_i(nblocks, per);
-    const size_t need = 2 * sg::Carver::need(size_t(nblocks) * n_cols * sizeof(float)) +
-                        2 * sg::Carver::need(size_t(ngroups) * n_cols * sizeof(double));
+    ngroups = colsum ? sg::ceil_div_i(nblocks, per) : 0;
+    const size_t need = (colsum ? 2 * sg::Carver::need(size_t(nblocks) * n_cols * sizeof(float)) +
+                                      2 * sg::Carver::need(size_t(ngroups) * n_cols * sizeof(double))
+                                : 0) +
+                        (narrow ? sg::Carver::need(size_t(n_genes) * sizeof(int16_t)) : 0) + 256;
     int status;
     void* w = sg::ws_get(h, need, &status);
     if (!w) return status;
     sg::Carver cv(w);
-    ps = cv.take<float>(size_t(nblocks) * n_cols);
-    pq = cv.take<float>(size_t(nblocks) * n_cols);
-    gs = cv.take<double>(size_t(ngroups) * n_cols);
-    gq = cv.take<double>(size_t(ngroups) * n_cols);
+    if (colsum) {
+      ps = cv.take<float>(size_t(nblocks) * n_cols);
+      pq = cv.take<float>(size_t(nblocks) * n_cols);
+      gs = cv.take<double>(size_t(ngroups) * n_cols);
+      gq = cv.take<double>(size_t(ngroups) * n_cols);
+    }
+    if (narrow) map16 = cv.take<int16_t>(size_t(n_genes));
   }
+  if (narrow) {
+    narrow_map_kernel<<<sg::ceil_div_i(n_genes, 256), 256, 0, st>>>(col_map, n_genes, n_cols, map16);
+    SG_LAUNCH_CHECK();
+  }
+  // 16-byte loads need indices and counts equally aligned
+  const int vec = ((reinterpret_cast<uintptr_t>(indices) ^ reinterpret_cast<uintptr_t>(data)) & 15) == 0 ? 1 : 0;
   const float sf = float(size_factor);
   sg::ProfScope prof(h, "normalize", st);
-  if (out_dtype == SG_F32) {
-    SG_CUDA(cudaFuncSetAttribute(normalize_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    normalize_kernel<false><<<nblocks, nwarps * 32, smem, st>>>(
-        indptr, indices, data, n_rows, col_map, n_genes, n_cols, pitch, missing_mask, fill_value, n_counts, sf,
-        flags, out, ld_out, libsize_out, ps, pq);
-  } else {
-    SG_CUDA(cudaFuncSetAttribute(normalize_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    normalize_kernel<true><<<nblocks, nwarps * 32, smem, st>>>(
-        indptr, indices, data, n_rows, col_map, n_genes, n_cols, pitch, missing_mask, fill_value, n_counts, sf,
-        flags, out, ld_out, libsize_out, ps, pq);
-  }
-  SG_LAUNCH_CHECK();
+  auto launch = [&](auto kern, const auto* map) -> int {
+    SG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    kern<<<nblocks, nwarps * 32, smem, st>>>(indptr, indices, data, n_rows, map, n_genes, n_cols, vec, pitch,
+                                             missing_mask, fill_value, n_counts, sf, flags, out, ld_out, libsize_out,
+                                             ps, pq);
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+  };
+  int rc;
+  if (out_dtype == SG_F32)
+    rc = narrow ? launch(normalize_kernel<false, int16_t>, map16) : launch(normalize_kernel<false, int32_t>, col_map);
+  else
+    rc = narrow ? launch(normalize_kernel<true, int16_t>, map16) : launch(normalize_kernel<true, int32_t>, col_map);
+  if (rc) return rc;
   if (colsum) {
     dim3 g1(sg::ceil_div_i(n_cols, 256), ngroups);
     partial_reduce1<<<g1, 256, 0, st>>>(ps, pq, nblocks, n_cols, per, gs, gq);

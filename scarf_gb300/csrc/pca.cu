@@ -8,6 +8,7 @@
 // applied while staging each 16-row slab into shared memory.
 #include "common.cuh"
 
+#include <cublas_v2.h>
 #include <cusolverDn.h>
 
 #include <algorithm>
@@ -231,6 +232,16 @@ __global__ void basis_kernel(const double* __restrict__ V, const double* __restr
   }
 }
 
+__global__ void f64_to_f32_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t ne) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e < ne) b[e] = float(a[e]);
+}
+
+__global__ void f32_to_f64_kernel(const float* __restrict__ a, double* __restrict__ b, int64_t ne) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e < ne) b[e] = double(a[e]);
+}
+
 // ---- projection -----------------------------------------------------------
 constexpr int PR = 128;  // rows per CTA
 constexpr int PC = 64;   // output columns per CTA
@@ -315,6 +326,8 @@ int sg_cov_reduce(const float* part, int nsplit, int n_pad, int n_cols, double* 
 }
 
 void sg_solver_destroy(sg_handle* h) {
+  if (h->blas) cublasDestroy(static_cast<cublasHandle_t>(h->blas));
+  h->blas = nullptr;
   if (h->solver) cusolverDnDestroy(static_cast<cusolverDnHandle_t>(h->solver));
   if (h->solver_work) cudaFree(h->solver_work);
   h->solver = nullptr;
@@ -418,6 +431,127 @@ extern "C" int sg_pca_basis(sg_handle* h, const double* cov, const double* zsum,
   if (hinfo != 0) return sg::fail(SG_ERR_CUDA, "cusolverDnDsyevdx: info=%d", hinfo);
   if (meig != n_comp) return sg::fail(SG_ERR_CUDA, "cusolverDnDsyevdx returned %d of %d eigenpairs", meig, n_comp);
   basis_kernel<<<n_comp, 256, 0, st>>>(A, W, n, n_comp, tr, comps, evals, evr, n_load, loadings32, ld_l);
+  SG_LAUNCH_CHECK();
+  SG_CUDA(cudaStreamSynchronize(st));
+  return SG_OK;
+}
+
+namespace {
+
+int solver_work(sg_handle* h, size_t wbytes) {
+  if (h->solver_work_bytes >= wbytes) return SG_OK;
+  if (h->solver_work) cudaFree(h->solver_work);
+  h->solver_work = nullptr;
+  h->solver_work_bytes = 0;
+  if (h->budget && wbytes + h->ws_bytes > h->budget)
+    return sg::fail(SG_ERR_BUDGET, "eigensolver workspace of %zu bytes exceeds the HBM budget", wbytes);
+  SG_CUDA(cudaMalloc(&h->solver_work, wbytes));
+  h->solver_work_bytes = wbytes;
+  return SG_OK;
+}
+
+#define SG_BLAS(call)                                                                              \
+  do {                                                                                             \
+    cublasStatus_t s_ = (call);                                                                    \
+    if (s_ != CUBLAS_STATUS_SUCCESS) return sg::fail(SG_ERR_CUDA, "%s failed (status %d)", #call, int(s_)); \
+  } while (0)
+#define SG_SOLVER(call)                                                                            \
+  do {                                                                                             \
+    cusolverStatus_t s_ = (call);                                                                  \
+    if (s_ != CUSOLVER_STATUS_SUCCESS) return sg::fail(SG_ERR_CUDA, "%s failed (status %d)", #call, int(s_)); \
+  } while (0)
+
+}  // namespace
+
+// Mixed-precision principal axes: an FP32 partial eigendecomposition of the
+// centred scatter (top n_comp + 16 pairs), then an FP64 Rayleigh-Ritz step on
+// that subspace (FP64 Cholesky-QR orthonormalisation, FP64 Q^T A Q and its
+// FP64 eigendecomposition), so eigenvalues and vectors are FP64 Ritz pairs.
+extern "C" int sg_pca_basis_mixed(sg_handle* h, const double* cov, const double* zsum, int64_t n_used,
+                                  int32_t n_cols, int32_t n_comp, double* comps, double* evals, double* evr,
+                                  int32_t n_load, float* loadings32, int32_t ld_l, void* stream) {
+  SG_HANDLE_CHECK(h);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  SG_ARG(cov && comps && n_cols > 0 && n_used > 0, "sg_pca_basis_mixed: bad arguments");
+  SG_ARG(n_comp >= 1 && n_comp <= n_cols, "sg_pca_basis_mixed: n_comp=%d outside [1, %d]", n_comp, n_cols);
+  SG_ARG(!loadings32 || (n_load >= 0 && n_load <= n_comp && ld_l >= n_load),
+         "sg_pca_basis_mixed: bad loadings shape");
+  const int n = n_cols;
+  const int m = std::min(n, n_comp + 16);
+  if (!h->solver) {
+    cusolverDnHandle_t s;
+    SG_SOLVER(cusolverDnCreate(&s));
+    h->solver = s;
+  }
+  if (!h->blas) {
+    cublasHandle_t b;
+    SG_BLAS(cublasCreate(&b));
+    h->blas = b;
+  }
+  cusolverDnHandle_t sol = static_cast<cusolverDnHandle_t>(h->solver);
+  cublasHandle_t blas = static_cast<cublasHandle_t>(h->blas);
+  SG_SOLVER(cusolverDnSetStream(sol, st));
+  SG_BLAS(cublasSetStream(blas, st));
+  const size_t nn = size_t(n) * n, nm = size_t(n) * m, mm = size_t(m) * m;
+  const size_t need = sg::Carver::need(nn * 8) + sg::Carver::need(nn * 4) + 3 * sg::Carver::need(nm * 8) +
+                      2 * sg::Carver::need(mm * 8) + 2 * sg::Carver::need(size_t(n) * 8) + 1024;
+  int status;
+  void* w = sg::ws_get(h, need, &status);
+  if (!w) return status;
+  sg::Carver cv(w);
+  double* A = cv.take<double>(nn);
+  float* A32 = cv.take<float>(nn);
+  double* Q = cv.take<double>(nm);
+  double* Y = cv.take<double>(nm);
+  double* V = cv.take<double>(nm);
+  double* G = cv.take<double>(mm);
+  double* B = cv.take<double>(mm);
+  float* W32 = cv.take<float>(n);
+  double* W = cv.take<double>(n);
+  double* tr = cv.take<double>(1);
+  int* info = cv.take<int>(1);
+  const int64_t ne = int64_t(nn);
+  center_kernel<<<sg::ceil_div_i(ne, 256), 256, 0, st>>>(cov, zsum, 1.0 / double(n_used), n, A);
+  SG_LAUNCH_CHECK();
+  trace_kernel<<<1, 256, 0, st>>>(A, n, tr);
+  SG_LAUNCH_CHECK();
+  f64_to_f32_kernel<<<sg::ceil_div_i(ne, 256), 256, 0, st>>>(A, A32, ne);
+  SG_LAUNCH_CHECK();
+  sg::ProfScope prof(h, "eigh", st);
+  const int il = n - m + 1, iu = n;
+  int meig = 0, lwork = 0;
+  SG_SOLVER(cusolverDnSsyevdx_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER,
+                                         n, A32, n, 0.f, 0.f, il, iu, &meig, W32, &lwork));
+  int lwork_d = 0;
+  SG_SOLVER(cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, B, m, W, &lwork_d));
+  const size_t wb = std::max(sizeof(float) * size_t(lwork), sizeof(double) * size_t(lwork_d));
+  int rc = solver_work(h, wb);
+  if (rc) return rc;
+  SG_SOLVER(cusolverDnSsyevdx(sol, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER, n, A32, n,
+                              0.f, 0.f, il, iu, &meig, W32, static_cast<float*>(h->solver_work), lwork, info));
+  if (meig != m) return sg::fail(SG_ERR_CUDA, "cusolverDnSsyevdx returned %d of %d eigenpairs", meig, m);
+  f32_to_f64_kernel<<<sg::ceil_div_i(int64_t(nm), 256), 256, 0, st>>>(A32, Q, int64_t(nm));
+  SG_LAUNCH_CHECK();
+  const double one = 1.0, zero = 0.0;
+  // Q <- Q R^-1 with Q^T Q = L L^T (R = L^T): FP64 Cholesky-QR
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Q, n, Q, n, &zero, G, m));
+  SG_SOLVER(cusolverDnDpotrf(sol, CUBLAS_FILL_MODE_LOWER, m, G, m, static_cast<double*>(h->solver_work),
+                             int(h->solver_work_bytes / sizeof(double)), info));
+  SG_BLAS(cublasDtrsm(blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, m, &one, G,
+                      m, Q, n));
+  // Rayleigh quotient B = Q^T A Q and its FP64 eigendecomposition
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &one, A, n, Q, n, &zero, Y, n));
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Q, n, Y, n, &zero, B, m));
+  SG_SOLVER(cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, B, m, W,
+                             static_cast<double*>(h->solver_work), lwork_d, info));
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, Q, n, B, m, &zero, V, n));
+  int hinfo = 0;
+  SG_CUDA(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(cudaStreamSynchronize(st));
+  if (hinfo != 0) return sg::fail(SG_ERR_CUDA, "sg_pca_basis_mixed: factorisation info=%d", hinfo);
+  // the n_comp largest Ritz pairs are the last n_comp columns (ascending order)
+  basis_kernel<<<n_comp, 256, 0, st>>>(V + size_t(m - n_comp) * n, W + (m - n_comp), n, n_comp, tr, comps, evals,
+                                       evr, n_load, loadings32, ld_l);
   SG_LAUNCH_CHECK();
   SG_CUDA(cudaStreamSynchronize(st));
   return SG_OK;

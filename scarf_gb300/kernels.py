@@ -166,8 +166,10 @@ def covariance(x: torch.Tensor, mu32: torch.Tensor, sigma32: torch.Tensor, n_col
 
 
 def pca_basis(cov: torch.Tensor, zsum: Optional[torch.Tensor], n_used: int, n_comp: int,
-              n_load: Optional[int] = None, ld_l: Optional[int] = None):
-    """a4: top ``n_comp`` principal axes (FP64 eigh on the device, svd_flip signs).
+              n_load: Optional[int] = None, ld_l: Optional[int] = None, eigh: str = "fp64"):
+    """a4: top ``n_comp`` principal axes on the device, svd_flip signs.
+    ``eigh='fp64'``: FP64 partial eigendecomposition of the whole scatter;
+    ``eigh='mixed'``: FP32 partial eigendecomposition + FP64 Rayleigh-Ritz.
 
     Returns ``(comps h x n_comp f64, evals, evr, loadings32 h x ld_l)`` where
     loadings32 holds the first ``n_load`` (default n_comp - 1) components."""
@@ -180,8 +182,9 @@ def pca_basis(cov: torch.Tensor, zsum: Optional[torch.Tensor], n_used: int, n_co
     evals = torch.empty(n_comp, dtype=torch.float64, device=dev)
     evr = torch.empty(n_comp, dtype=torch.float64, device=dev)
     l32 = torch.empty((h, ld_l), dtype=torch.float32, device=dev)
-    L.check(L.load().sg_pca_basis(handle(dev.index).ptr, _p(cov), _p(zsum), int(n_used), h, n_comp, _p(comps),
-                                  _p(evals), _p(evr), n_load, _p(l32), ld_l, _stream(dev)))
+    fn = {"fp64": L.load().sg_pca_basis, "mixed": L.load().sg_pca_basis_mixed}[eigh]
+    L.check(fn(handle(dev.index).ptr, _p(cov), _p(zsum), int(n_used), h, n_comp, _p(comps), _p(evals), _p(evr),
+               n_load, _p(l32), ld_l, _stream(dev)))
     return comps, evals, evr, l32
 
 

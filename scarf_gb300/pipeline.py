@@ -144,11 +144,14 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k:
                log_transform: bool = True, renormalize_subset: bool = True, n_counts=None,
                use_for_pca: Optional[np.ndarray] = None, chunk_cells: Optional[int] = None,
                smooth: bool = True, keep_x: bool = True, cov_form: Optional[str] = None,
-               device="cuda") -> GraphResult:
+               eigh: Optional[str] = None, device="cuda") -> GraphResult:
     """The whole path on the device; returns device tensors.
 
-    ``precision`` selects the kNN form; ``cov_form`` the covariance form
-    (default: the same as ``precision`` where that form is built)."""
+    ``precision`` selects the form: "plain" (FP32 scatter, FP32 kNN, full FP64
+    eigendecomposition) or "precision" (3xBF16 scatter, BF16 tcgen05 kNN with
+    FP32 re-rank, FP32 partial eigendecomposition refined by an FP64
+    Rayleigh-Ritz step). ``cov_form`` and ``eigh`` override the scatter form
+    and the eigensolver ("fp64" or "mixed")."""
     dev = torch.device(device)
     n = len(indptr) - 1
     h = len(feat_idx)
@@ -167,7 +170,9 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k:
     if cov_form is None:
         cov_form = precision if precision in COV_FORMS else "plain"
     cov, zsum = K.covariance(x, mu32, sigma32, n_cols=h, row_mask=mask, precision=cov_form)
-    comps, evals, evr, l32 = K.pca_basis(cov, zsum, n_used, dims + 1, n_load=dims, ld_l=dims)
+    if eigh is None:
+        eigh = "mixed" if precision == "precision" else "fp64"
+    comps, evals, evr, l32 = K.pca_basis(cov, zsum, n_used, dims + 1, n_load=dims, ld_l=dims, eigh=eigh)
     scores = K.project(x, mu32, sigma32, l32, dims, n_cols=h)
     if margin is None:
         margin = PRECISION_MARGIN if precision == "precision" else PLAIN_MARGIN

@@ -165,6 +165,42 @@ class BatchScheduler:
             self.lock.notify_all()
 
 
+class Reference:
+    """Device-resident mapping reference: z-scale statistics, loadings and the
+    reference cells' scores, with the query form ("plain" or "precision").
+    ``from_graph`` takes them from a ``pipeline.GraphResult``; an ``AnnStream``
+    carries the same attributes and can be used in its place."""
+
+    def __init__(self, mu32, sigma32, loadings32, dims: int, scores, n_feats: int, precision: str = "precision",
+                 margin: Optional[int] = None):
+        from .ann import GpuExactIndex, NormalizedData
+        self._mu32, self._sg32, self._l32 = mu32, sigma32, loadings32
+        self.dims = int(dims)
+        self.nFeats = int(n_feats)
+        self.data = NormalizedData(scores, n_feats, 1)  # only .x.device is read
+        self.annIdx = GpuExactIndex("l2", dims, precision=precision, margin=margin, device=scores.device)
+        self.annIdx._rows = [scores]
+
+    @classmethod
+    def from_graph(cls, g, precision: str = "precision", margin: Optional[int] = None) -> "Reference":
+        return cls(g.mu32, g.sigma32, g.loadings32.contiguous(), g.dims, g.scores, g.n_feats, precision, margin)
+
+
+class _Staging:
+    """Pinned host buffers of one worker, grown on demand."""
+
+    def __init__(self):
+        self.bufs = {}
+
+    def get(self, name, n, dtype):
+        import torch
+        b = self.bufs.get(name)
+        if b is None or b.numel() < n:
+            b = torch.empty(max(n, 1024) * 5 // 4, dtype=dtype, pin_memory=True)
+            self.bufs[name] = b
+        return b[:n]
+
+
 class MappingServer:
     """GPU executor of the scheduler's batches (see the module docstring).
 
@@ -234,6 +270,7 @@ class MappingServer:
         from . import kernels as K
         torch.cuda.set_device(self.device)
         stream = torch.cuda.Stream(self.device)
+        stage = _Staging()
         ref = self.ref
         h = ref.nFeats
         while True:
@@ -244,18 +281,24 @@ class MappingServer:
                 continue
             try:
                 ip, ind, dat = _concat_rows(batch)
+                p_ip = stage.get("ip", len(ip), torch.int64)
+                p_ind = stage.get("ind", len(ind), torch.int32)
+                p_dat = stage.get("dat", len(dat), torch.int32)
+                p_ip.numpy()[:] = ip
+                p_ind.numpy()[:] = ind
+                p_dat.numpy()[:] = dat
                 with torch.cuda.stream(stream):
-                    t_ip = torch.from_numpy(ip).pin_memory().to(self.device, non_blocking=True)
-                    t_ind = torch.from_numpy(ind).pin_memory().to(self.device, non_blocking=True)
-                    t_dat = torch.from_numpy(dat).pin_memory().to(self.device, non_blocking=True)
+                    t_ip = p_ip.to(self.device, non_blocking=True)
+                    t_ind = p_ind.to(self.device, non_blocking=True)
+                    t_dat = p_dat.to(self.device, non_blocking=True)
                     x = K.normalize_csr(t_ip, t_ind, t_dat, self.cmap, h, size_factor=self.size_factor,
                                         log_transform=self.log_transform, renormalize_subset=self.renorm,
                                         missing_mask=self.missing, fill_value=1.0)
                     s = K.project(x, ref._mu32, ref._sg32, ref._l32, ref.dims, n_cols=h)
                     idx, dist, _ = K.knn(s, ref.annIdx.scores, ref.dims, self.k, self_offset=-1,
                                          margin=ref.annIdx._margin(), precision=self.precision)
-                    hi = torch.empty(idx.shape, dtype=idx.dtype, pin_memory=True)
-                    hd = torch.empty(dist.shape, dtype=dist.dtype, pin_memory=True)
+                    hi = stage.get("oi", idx.numel(), idx.dtype).view(idx.shape)
+                    hd = stage.get("od", dist.numel(), dist.dtype).view(dist.shape)
                     hi.copy_(idx, non_blocking=True)
                     hd.copy_(dist, non_blocking=True)
                 stream.synchronize()

@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import math
 from dataclasses import dataclass
+from typing import Optional
 
 import numpy as np
 import torch
@@ -34,7 +35,10 @@ class CountsCSR:
 
 def nb_counts(n_cells: int, n_genes: int, n_clusters: int, seed: int, lib_median: float = 3000.0,
               lib_sigma: float = 0.35, dispersion: float = 0.5, genes_per_cluster: int = 100,
-              device: str = "cpu", chunk: int = 4096) -> CountsCSR:
+              device: str = "cpu", chunk: int = 4096, cells_seed: Optional[int] = None) -> CountsCSR:
+    """``seed`` fixes the population (gene means, cluster programmes);
+    ``cells_seed`` (default: the same) fixes the cells drawn from it, so that
+    query cells of the same populations can be drawn apart from a reference."""
     dev = torch.device(device)
     g = torch.Generator(device=dev)
     g.manual_seed(int(seed))
@@ -46,6 +50,8 @@ def nb_counts(n_cells: int, n_genes: int, n_clusters: int, seed: int, lib_median
         prog[c, idx] = 2.0 + 2.0 * torch.rand(idx.numel(), generator=g, device=dev, dtype=torch.float64)
     prob = gene_mu[None, :] * prog
     prob = (prob / prob.sum(1, keepdim=True)).to(f32)
+    if cells_seed is not None and cells_seed != seed:
+        g.manual_seed(int(cells_seed) * 7919 + 17)
     labels = torch.randint(0, n_clusters, (n_cells,), generator=g, device=dev)
     lib = torch.exp(math.log(lib_median) + lib_sigma * torch.randn(n_cells, generator=g, device=dev))
     shape = 1.0 / dispersion

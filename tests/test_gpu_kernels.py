@@ -145,6 +145,19 @@ def test_covariance_precision(K, counts):
     assert oracle.subspace_angles(comps.cpu().numpy()[:, :5], ocomp[:, :5]).max() < 1e-3
 
 
+def test_pca_basis_mixed_matches_fp64(K, counts):
+    x, cs, cq, _ = _normalize(K, counts)
+    mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
+    cov, zsum = K.covariance(x, mu32, sg32, n_cols=len(counts[4]))
+    a = K.pca_basis(cov, zsum, x.shape[0], 21, n_load=20, ld_l=20)
+    b = K.pca_basis(cov, zsum, x.shape[0], 21, n_load=20, ld_l=20, eigh="mixed")
+    ca, cb = a[0].cpu().numpy(), b[0].cpu().numpy()
+    assert np.allclose(a[1].cpu().numpy(), b[1].cpu().numpy(), rtol=1e-5)
+    assert oracle.subspace_angles(ca[:, :20], cb[:, :20]).max() < 1e-3
+    for j in range(3):                      # separated leading components agree one by one, signs included
+        assert np.abs(ca[:, j] - cb[:, j]).max() < 1e-4
+
+
 def test_pca_basis_and_projection(K, counts):
     x, cs, cq, _ = _normalize(K, counts)
     mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
