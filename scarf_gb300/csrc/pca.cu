@@ -316,14 +316,6 @@ __global__ void pad_cols_kernel(float* __restrict__ s, int64_t n_rows, int from,
 
 }  // namespace
 
-// FP64 reduction (fixed order over splits) of float32 partial scatters laid
-// out as [nsplit][n_pad][n_pad]; the upper triangle is added to cov and mirrored.
-int sg_cov_reduce(const float* part, int nsplit, int n_pad, int n_cols, double* cov, cudaStream_t st) {
-  const int T = n_pad / CT;
-  cov_reduce_kernel<<<T * (T + 1) / 2, 256, 0, st>>>(part, nsplit, n_pad, n_cols, T, cov);
-  SG_LAUNCH_CHECK();
-  return SG_OK;
-}
 
 void sg_solver_destroy(sg_handle* h) {
   if (h->blas) cublasDestroy(static_cast<cublasHandle_t>(h->blas));

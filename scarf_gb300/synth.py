@@ -27,6 +27,10 @@ class CountsCSR:
     n_cells: int
     n_genes: int
     labels: np.ndarray   # int32 cluster of each cell
+    # per-gene sums of log1p(1000 c / library size) and of its square, taken
+    # while the counts were drawn (what select_hvgs ranks by)
+    gene_s1: Optional[np.ndarray] = None
+    gene_s2: Optional[np.ndarray] = None
 
     @property
     def nnz(self) -> int:
@@ -57,11 +61,18 @@ def nb_counts(n_cells: int, n_genes: int, n_clusters: int, seed: int, lib_median
     shape = 1.0 / dispersion
     ptr_parts, ind_parts, dat_parts = [], [], []
     counts_per_row = []
+    s1 = torch.zeros(n_genes, dtype=torch.float64, device=dev)
+    s2 = torch.zeros(n_genes, dtype=torch.float64, device=dev)
     for s in range(0, n_cells, chunk):
         e = min(n_cells, s + chunk)
         mu = lib[s:e, None] * prob[labels[s:e]]
         gam = torch._standard_gamma(torch.full_like(mu, shape), generator=g) / shape
         cnt = torch.poisson(mu * gam, generator=g).to(torch.int32)
+        tot = cnt.sum(1, keepdim=True).clamp_min(1).double()
+        xl = torch.log1p(1000.0 * cnt.double() / tot)
+        s1 += xl.sum(0)
+        s2 += (xl * xl).sum(0)
+        del xl, tot
         nz = cnt.nonzero()
         ind_parts.append(nz[:, 1].to(torch.int32).cpu())
         dat_parts.append(cnt[nz[:, 0], nz[:, 1]].cpu())
@@ -71,12 +82,16 @@ def nb_counts(n_cells: int, n_genes: int, n_clusters: int, seed: int, lib_median
     indptr = np.zeros(n_cells + 1, dtype=np.int64)
     np.cumsum(per_row, out=indptr[1:])
     return CountsCSR(indptr=indptr, indices=torch.cat(ind_parts).numpy(), data=torch.cat(dat_parts).numpy(),
-                     n_cells=n_cells, n_genes=n_genes, labels=labels.cpu().numpy().astype(np.int32))
+                     n_cells=n_cells, n_genes=n_genes, labels=labels.cpu().numpy().astype(np.int32),
+                     gene_s1=s1.cpu().numpy(), gene_s2=s2.cpu().numpy())
 
 
 def select_hvgs(csr: CountsCSR, n_top: int, size_factor: float = 1000.0) -> np.ndarray:
     """Sorted indices of the ``n_top`` genes of largest variance of
     log1p(size_factor * c / library size) (library size over all genes)."""
+    if csr.gene_s1 is not None and size_factor == 1000.0:
+        var = csr.gene_s2 / csr.n_cells - (csr.gene_s1 / csr.n_cells) ** 2
+        return np.sort(np.argsort(-var, kind="stable")[:n_top]).astype(np.int64)
     lib = np.diff(np.concatenate([[0], np.cumsum(csr.data, dtype=np.int64)])[csr.indptr])
     lib = np.maximum(lib, 1).astype(np.float64)
     rows = np.repeat(np.arange(csr.n_cells), np.diff(csr.indptr))

@@ -145,6 +145,40 @@ def test_covariance_precision(K, counts):
     assert oracle.subspace_angles(comps.cpu().numpy()[:, :5], ocomp[:, :5]).max() < 1e-3
 
 
+def test_covariance_long_accumulation(K):
+    # 600,000 rows of sparse columns: the zero entries of a column give one
+    # repeated z value, whose products all round the same way in a long FP32
+    # accumulation. Both scatters stay within their bounds of an FP64 scatter
+    # of the same z = (x - mu32)/sigma32.
+    g = torch.Generator(device="cuda").manual_seed(11)
+    n, h = 600_000, 512
+    dens = torch.linspace(0.05, 0.9, h, device="cuda", dtype=torch.float64)
+    x = torch.empty((n, h), dtype=torch.float32, device="cuda")
+    for a in range(0, n, 100_000):
+        u = torch.rand((100_000, h), generator=g, device="cuda", dtype=torch.float64)
+        v = torch.log1p(20.0 * torch.rand((100_000, h), generator=g, device="cuda", dtype=torch.float64))
+        x[a:a + 100_000] = torch.where(u < dens[None, :], v, torch.zeros_like(v)).float()
+    mu = x.double().mean(0)
+    sg = x.double().std(0, unbiased=False)
+    mu32, sg32 = mu.float(), sg.float()
+    want = torch.zeros((h, h), dtype=torch.float64, device="cuda")
+    zs = torch.zeros(h, dtype=torch.float64, device="cuda")
+    for a in range(0, n, 100_000):
+        z = (x[a:a + 100_000].double() - mu32.double()) / sg32.double()
+        want += z.T @ z
+        zs += z.sum(0)
+    scale = float(want.abs().max())
+    err = {}
+    for form in ("plain", "precision"):
+        cov, zsum = K.covariance(x, mu32, sg32, n_cols=h, precision=form)
+        torch.cuda.synchronize()
+        err[form] = float((cov - want).abs().max()) / scale
+        assert float((zsum - zs).abs().max()) < 1.0
+    print("relative max-abs scatter error", err)
+    assert err["precision"] <= 1.2e-5
+    assert err["plain"] <= 1.2e-4
+
+
 def test_pca_basis_mixed_matches_fp64(K, counts):
     x, cs, cq, _ = _normalize(K, counts)
     mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
