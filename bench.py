@@ -659,6 +659,8 @@ def run_serve(args):
             r.result(timeout=600)
         t_end = max(r.t_done for r in reqs)
         batches = srv.batches_run
+        blog = np.array(srv.batch_log[3:], dtype=np.float64).reshape(-1, 2)
+        ulog = np.array(srv.upload_log[3:], dtype=np.float64).reshape(-1, 2)
     summ = latency_summary(reqs)
     small = latency_summary([r for r in reqs if r.n_cells <= 10_000])
     # recall of one mid-size request against exact FP64 kNN on the device
@@ -685,6 +687,11 @@ def run_serve(args):
         "p50_ms_requests_le_10k_cells": round(small.get("p50_ms", float("nan")), 3),
         "requests": summ["requests"], "cells": summ["cells"],
         "cells_per_s": round(summ["cells"] / (t_end - t0), 1), "gpu_batches": batches,
+        "batch_rows_mean": round(float(blog[:, 0].mean()), 1) if len(blog) else None,
+        "batch_ms_p50": round(float(np.percentile(blog[:, 1], 50)) * 1e3, 3) if len(blog) else None,
+        "batch_ms_p99": round(float(np.percentile(blog[:, 1], 99)) * 1e3, 3) if len(blog) else None,
+        "upload_ms_p50": round(float(np.percentile(ulog[:, 1], 50)) * 1e3, 3) if len(ulog) else None,
+        "upload_ms_p99": round(float(np.percentile(ulog[:, 1], 99)) * 1e3, 3) if len(ulog) else None,
         "recall_at_k_sampled_request": round(rec, 5), "data": "synthetic",
         "config": {"workload": c["name"], "arrival_rate_hz": c["rate_hz"], "max_batch_rows": c["max_batch_rows"],
                    "workers": 2, "form": "precision"}}), flush=True)

@@ -10,23 +10,30 @@ Scheduling (``BatchScheduler``, pure host logic):
 * requests are admitted in arrival order while the HBM they need (their CSR,
   normalised rows, scores and results) fits the budget; a request that cannot
   fit the budget alone is rejected with ``MemoryError``;
-* each GPU batch takes up to ``max_batch_rows`` rows from the admitted
-  requests, oldest first, so a large request is processed in row slices and
-  requests that arrive while it is on the GPU join the next batches instead of
-  waiting for it to finish;
+* an admitted request is handed to the uploader, which copies its CSR to the
+  device once; it is ready for batching when that copy has landed;
+* each GPU batch takes up to ``max_batch_rows`` rows from the ready requests,
+  shortest remaining first (ties by arrival), so a large request is processed
+  in row slices and a small request that arrives while it is on the GPU goes
+  into the next batch instead of waiting for it to finish;
 * a request completes when all its rows are back; its memory is released and
   the next queued requests are admitted.
 
-Execution (``MappingServer``): ``n_workers`` host threads, each with its own
-CUDA stream and library handle, take batches from the scheduler; the copies
-and kernels of different batches overlap on the device. Rows are independent,
-so a request's result does not depend on what it was batched with.
+Execution (``MappingServer``): uploader threads (smallest request first) copy
+admitted requests to the device; ``n_workers``
+host threads, each with its own CUDA stream and library handle, take batches
+from the scheduler and assemble each batch's CSR on the device from the
+resident requests. The copies and kernels of different batches overlap on the
+device. Rows are independent, so a request's result does not depend on what it
+was batched with.
 """
 from __future__ import annotations
 
 import collections
+import heapq
 import threading
 import time
+import warnings
 from dataclasses import dataclass, field
 from typing import Deque, List, Optional, Tuple
 
@@ -50,6 +57,8 @@ class MapRequest:
     t_done: Optional[float] = None
     error: Optional[BaseException] = None
     done: threading.Event = field(default_factory=threading.Event)
+    ready: bool = True                 # CSR resident where the batches read it
+    dev: Optional[tuple] = None        # device (indptr, indices, data)
 
     def __post_init__(self):
         self.n_cells = len(self.indptr) - 1
@@ -72,7 +81,11 @@ Slice = Tuple[MapRequest, int, int]
 class BatchScheduler:
     """HBM-budget admission and row-sliced continuous batching (host only)."""
 
-    def __init__(self, hbm_budget_bytes: int, max_batch_rows: int, bytes_per_row: int, bytes_per_nnz: int = 8):
+    def __init__(self, hbm_budget_bytes: int, max_batch_rows: int, bytes_per_row: int, bytes_per_nnz: int = 8,
+                 uploader=None):
+        """``uploader(req)``, when given, is called (outside the lock) for each
+        admitted request, which becomes ready when ``mark_ready`` is called."""
+        self.uploader = uploader
         self.budget = int(hbm_budget_bytes)
         self.max_rows = int(max_batch_rows)
         self.bytes_per_row = int(bytes_per_row)
@@ -102,34 +115,64 @@ class BatchScheduler:
                 req.done.set()
                 return req
             self.queued.append(req)
-            self._admit()
+            new = self._admit()
             self.lock.notify_all()
+        self._upload(new)
         return req
 
-    def _admit(self):
+    def _admit(self) -> List[MapRequest]:
+        new = []
         while self.queued and self.in_use + self.queued[0].bytes_needed <= self.budget:
             r = self.queued.popleft()
             self.in_use += r.bytes_needed
             r.idx = np.empty((r.n_cells, r.k), np.int64)
             r.dist = np.empty((r.n_cells, r.k), np.float32)
+            r.ready = self.uploader is None
             self.active.append(r)
+            new.append(r)
+        return new
+
+    def _upload(self, reqs: List[MapRequest]):
+        if self.uploader is not None:
+            for r in reqs:
+                self.uploader(r)
+
+    def mark_ready(self, req: MapRequest, error: Optional[BaseException] = None):
+        """The uploader's report: ``req`` is resident (or failed with ``error``)."""
+        new = []
+        with self.lock:
+            if error is None:
+                req.ready = True
+            else:
+                req.error = error
+                if req in self.active:
+                    self.active.remove(req)
+                    self.in_use -= req.bytes_needed
+                req.dev = None
+                req.t_done = time.perf_counter()
+                req.done.set()
+                new = self._admit()
+            self.lock.notify_all()
+        self._upload(new)
+
+    def _pending(self) -> List[MapRequest]:
+        return [r for r in self.active if r.ready and r.next_row < r.n_cells]
 
     def next_batch(self, timeout: Optional[float] = None) -> List[Slice]:
-        """Up to max_rows rows from the admitted requests, oldest first."""
+        """Up to max_rows rows from the ready requests, shortest remaining
+        first (ties: oldest first)."""
         with self.lock:
             end = None if timeout is None else time.perf_counter() + timeout
-            while not self.closed and not any(r.next_row < r.n_cells for r in self.active):
+            while not self.closed and not self._pending():
                 left = None if end is None else end - time.perf_counter()
                 if left is not None and left <= 0:
                     return []
                 self.lock.wait(left)
             batch: List[Slice] = []
             room = self.max_rows
-            for r in self.active:
+            for r in sorted(self._pending(), key=lambda q: (q.n_cells - q.next_row, q.arrival, q.rid)):
                 if room == 0:
                     break
-                if r.next_row >= r.n_cells:
-                    continue
                 take = min(room, r.n_cells - r.next_row)
                 batch.append((r, r.next_row, r.next_row + take))
                 r.next_row += take
@@ -150,14 +193,16 @@ class BatchScheduler:
                     r.error = error
                 off += n
                 r.rows_done += n
-                if r.rows_done == r.n_cells or error is not None:
+                if (r.rows_done == r.n_cells or error is not None) and not r.done.is_set():
                     if r in self.active:
                         self.active.remove(r)
                         self.in_use -= r.bytes_needed
+                    r.dev = None
                     r.t_done = now
                     r.done.set()
-            self._admit()
+            new = self._admit()
             self.lock.notify_all()
+        self._upload(new)
 
     def close(self):
         with self.lock:
@@ -210,7 +255,8 @@ class MappingServer:
 
     def __init__(self, reference, ref_feature_ids, target_gene_ids, k: int = 11, max_batch_rows: int = 16384,
                  hbm_budget_bytes: int = 8 << 30, n_workers: int = 2, size_factor: float = 1000.0,
-                 log_transform: bool = True, renormalize_subset: bool = True, precision: Optional[str] = None):
+                 log_transform: bool = True, renormalize_subset: bool = True, precision: Optional[str] = None,
+                 n_uploaders: int = 2):
         import torch
 
         from .datastore import align_col_map
@@ -228,12 +274,21 @@ class MappingServer:
         ld = (h + 3) // 4 * 4
         lds = (reference.dims + 3) // 4 * 4
         per_row = 8 + ld * 4 + lds * 4 + self.k * 12
-        self.sched = BatchScheduler(hbm_budget_bytes, max_batch_rows, per_row)
+        self.sched = BatchScheduler(hbm_budget_bytes, max_batch_rows, per_row, bytes_per_nnz=8,
+                                    uploader=self._enqueue_upload)
         self.n_workers = int(n_workers)
+        self.n_uploaders = max(1, int(n_uploaders))
         self._threads: List[threading.Thread] = []
         self._rid = 0
         self._rid_lock = threading.Lock()
+        self._up_heap: list = []
+        self._up_cv = threading.Condition()
+        self._stopping = False
         self.batches_run = 0
+        # (rows, seconds from batch taken to results on the host) per batch,
+        # (cells, seconds of the host-to-device copy) per request
+        self.batch_log: List[Tuple[int, float]] = []
+        self.upload_log: List[Tuple[int, float]] = []
 
     # -- client side ----------------------------------------------------------
     def submit(self, indptr, indices, data, arrival: Optional[float] = None) -> MapRequest:
@@ -245,6 +300,10 @@ class MappingServer:
         return self.sched.submit(req)
 
     def start(self):
+        for i in range(self.n_uploaders):
+            t = threading.Thread(target=self._uploader, name=f"sg-up-{i}", daemon=True)
+            t.start()
+            self._threads.append(t)
         for i in range(self.n_workers):
             t = threading.Thread(target=self._worker, name=f"sg-map-{i}", daemon=True)
             t.start()
@@ -253,6 +312,9 @@ class MappingServer:
 
     def stop(self):
         self.sched.close()
+        with self._up_cv:
+            self._stopping = True
+            self._up_cv.notify_all()
         for t in self._threads:
             t.join(timeout=30)
         self._threads = []
@@ -263,7 +325,70 @@ class MappingServer:
     def __exit__(self, *exc):
         self.stop()
 
+    # -- uploader side --------------------------------------------------------
+    def _enqueue_upload(self, req: MapRequest):
+        with self._up_cv:
+            heapq.heappush(self._up_heap, (req.n_cells, req.arrival, req.rid, req))
+            self._up_cv.notify()
+
+    def _uploader(self):
+        # Copies go straight from the request's (pageable) arrays: on a
+        # coherent CPU-GPU link they run at the copy engines' rate, where a
+        # pass through a pinned staging buffer would add a host memcpy.
+        import torch
+        torch.cuda.set_device(self.device)
+        stream = torch.cuda.Stream(self.device)
+        while True:
+            with self._up_cv:
+                while not self._up_heap and not self._stopping:
+                    self._up_cv.wait(0.05)
+                if not self._up_heap:
+                    return
+                req = heapq.heappop(self._up_heap)[3]
+            t0 = time.perf_counter()
+            try:
+                p0, p1 = int(req.indptr[0]), int(req.indptr[-1])
+                hs = [req.indptr, req.indices[p0:p1], req.data[p0:p1]]
+                if p1 == p0:  # keep the device pointers valid for an all-empty request
+                    hs[1], hs[2] = np.zeros(1, np.int32), np.zeros(1, np.int32)
+                with torch.cuda.stream(stream), warnings.catch_warnings():
+                    # read-only request arrays are only read here
+                    warnings.filterwarnings("ignore", message="The given NumPy array is not writable")
+                    dev = tuple(torch.from_numpy(np.ascontiguousarray(h)).to(self.device, non_blocking=True)
+                                for h in hs)
+                stream.synchronize()
+                req.dev = dev
+                self.upload_log.append((req.n_cells, time.perf_counter() - t0))
+                self.sched.mark_ready(req)
+            except BaseException as e:  # surfaces in MapRequest.result()
+                self.sched.mark_ready(req, error=e)
+
     # -- worker side ----------------------------------------------------------
+    def _batch_csr(self, batch: List[Slice], stage: "_Staging"):
+        """The batch's CSR on the device: views of the request when the batch
+        is one slice, else a device concatenation of the slices."""
+        import torch
+        if len(batch) == 1:
+            r, a, b = batch[0]
+            ip_d, ind_d, dat_d = r.dev
+            return ip_d[a:b + 1], ind_d, dat_d, int(r.indptr[a] - r.indptr[0])
+        ptrs, inds, dats = [np.zeros(1, np.int64)], [], []
+        base = 0
+        for r, a, b in batch:
+            q0 = int(r.indptr[0])
+            p0, p1 = int(r.indptr[a]) - q0, int(r.indptr[b]) - q0
+            ptrs.append((r.indptr[a + 1:b + 1] - q0 - p0 + base).astype(np.int64))
+            inds.append(r.dev[1][p0:p1])
+            dats.append(r.dev[2][p0:p1])
+            base += p1 - p0
+        ip = np.concatenate(ptrs)
+        h_ip = stage.get("ip", len(ip), torch.int64)
+        h_ip.numpy()[:] = ip
+        if base == 0:  # keep the device pointers valid for an all-empty batch
+            inds, dats = [torch.zeros(1, dtype=torch.int32, device=self.device)], \
+                [torch.zeros(1, dtype=torch.int32, device=self.device)]
+        return h_ip.to(self.device, non_blocking=True), torch.cat(inds), torch.cat(dats), 0
+
     def _worker(self):
         import torch
 
@@ -279,19 +404,11 @@ class MappingServer:
                 if self.sched.closed:
                     return
                 continue
+            t0 = time.perf_counter()
             try:
-                ip, ind, dat = _concat_rows(batch)
-                p_ip = stage.get("ip", len(ip), torch.int64)
-                p_ind = stage.get("ind", len(ind), torch.int32)
-                p_dat = stage.get("dat", len(dat), torch.int32)
-                p_ip.numpy()[:] = ip
-                p_ind.numpy()[:] = ind
-                p_dat.numpy()[:] = dat
                 with torch.cuda.stream(stream):
-                    t_ip = p_ip.to(self.device, non_blocking=True)
-                    t_ind = p_ind.to(self.device, non_blocking=True)
-                    t_dat = p_dat.to(self.device, non_blocking=True)
-                    x = K.normalize_csr(t_ip, t_ind, t_dat, self.cmap, h, size_factor=self.size_factor,
+                    t_ip, t_ind, t_dat, off = self._batch_csr(batch, stage)
+                    x = K.normalize_csr(t_ip, t_ind[off:], t_dat[off:], self.cmap, h, size_factor=self.size_factor,
                                         log_transform=self.log_transform, renormalize_subset=self.renorm,
                                         missing_mask=self.missing, fill_value=1.0)
                     s = K.project(x, ref._mu32, ref._sg32, ref._l32, ref.dims, n_cols=h)
@@ -303,6 +420,7 @@ class MappingServer:
                     hd.copy_(dist, non_blocking=True)
                 stream.synchronize()
                 self.batches_run += 1
+                self.batch_log.append((int(idx.shape[0]), time.perf_counter() - t0))
                 self.sched.complete(batch, hi.numpy(), hd.numpy())
             except BaseException as e:  # surfaces in MapRequest.result()
                 self.sched.complete(batch, None, None, error=e)

@@ -38,10 +38,10 @@ def test_large_requests_are_sliced_and_later_requests_join():
     b1 = s.next_batch(timeout=0)
     assert [(a, e) for _, a, e in b1] == [(0, 16)]
     small = s.submit(req(1, 4))          # arrives while the big request is on the GPU
-    b2 = s.next_batch(timeout=0)
-    assert [(x.rid, a, e) for x, a, e in b2] == [(0, 16, 32)]
+    b2 = s.next_batch(timeout=0)         # shortest remaining first: the small one leads
+    assert [(x.rid, a, e) for x, a, e in b2] == [(1, 0, 4), (0, 16, 28)]
     b3 = s.next_batch(timeout=0)
-    assert [(x.rid, a, e) for x, a, e in b3] == [(0, 32, 40), (1, 0, 4)]
+    assert [(x.rid, a, e) for x, a, e in b3] == [(0, 28, 40)]
     for b in (b1, b2, b3):
         finish(s, b)
     assert big.done.is_set() and small.done.is_set()
@@ -83,3 +83,29 @@ def test_next_batch_waits_for_work_and_close_wakes_it():
     assert got and got[0][0][2] == 3
     s.close()
     assert s.next_batch(timeout=0.1) == []
+
+
+def test_requests_wait_for_their_upload():
+    uploads = []
+    s = BatchScheduler(hbm_budget_bytes=1 << 20, max_batch_rows=16, bytes_per_row=1, uploader=uploads.append)
+    a = s.submit(req(0, 5))
+    b = s.submit(req(1, 3))
+    assert [r.rid for r in uploads] == [0, 1]
+    assert s.next_batch(timeout=0) == []          # nothing resident yet
+    s.mark_ready(b)
+    assert [(x.rid, lo, hi) for x, lo, hi in s.next_batch(timeout=0)] == [(1, 0, 3)]
+    s.mark_ready(a, error=IOError("copy failed"))
+    with pytest.raises(IOError):
+        a.result(timeout=1)
+    assert s.in_use == b.bytes_needed
+
+
+def test_failed_upload_admits_the_next_request():
+    uploads = []
+    cost = 10 * 1 + 30 * 8
+    s = BatchScheduler(hbm_budget_bytes=cost, max_batch_rows=16, bytes_per_row=1, uploader=uploads.append)
+    a = s.submit(req(0, 10))
+    b = s.submit(req(1, 10))
+    assert [r.rid for r in uploads] == [0] and [r.rid for r in s.queued] == [1]
+    s.mark_ready(a, error=RuntimeError("no memory"))
+    assert [r.rid for r in uploads] == [0, 1] and [r.rid for r in s.active] == [1]
