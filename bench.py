@@ -432,7 +432,7 @@ def run_gb300(args, cfg):
         "vs_baseline": None,
         "dtype": "bf16",
         "data": "synthetic (seeded negative-binomial counts generated on the device)",
-        "config": {"workload": cfg["name"], "form": "precision: 3xbf16 tcgen05 scatter, f32 partial eigh + f64 "
+        "config": {"workload": cfg["name"], "form": "precision: 3xbf16 tcgen05 scatter, chebyshev-filtered f32 eigh + f64 "
                    "Rayleigh-Ritz, bf16 tcgen05 distances, f32 re-rank", "margin": 16, "batch_size": BATCH,
                    "nnz": csr.nnz, "l2": "inputs larger than L2 (CSR %.2f GB, normalised matrix %.2f GB)"
                    % (h2d / 1e9, n * cfg["n_hvg"] * 4 / 1e9), "parallelism": f"replicas x{ws}"},
@@ -464,9 +464,10 @@ def run_gb300(args, cfg):
 
 
 def eigensolver_comparison(K, pipeline, ip, ind, dat, G, feat, n, dims, reps=3):
-    """FP64 partial eigendecomposition (the default) against the mixed FP32 +
-    FP64 Rayleigh-Ritz solver on this workload's scatter: device time of each
-    and the principal angles between their leading subspaces."""
+    """FP64 partial eigendecomposition (the plain form's solver) against the
+    mixed FP32 + FP64 Rayleigh-Ritz solver and the Chebyshev-filtered
+    subspace iteration on this workload's scatter: device time of each and the
+    principal angles between its leading subspace and the FP64 one."""
     import torch
     x, cs, cq = pipeline.normalize_csr_host(ip, ind, dat, G, feat, device=ip.device)
     mu, sg, mu32, sg32 = K.zstats(cs, cq, n)
@@ -474,7 +475,7 @@ def eigensolver_comparison(K, pipeline, ip, ind, dat, G, feat, n, dims, reps=3):
     del x
     out = {}
     comps = {}
-    for method in ("fp64", "mixed"):
+    for method in ("fp64", "mixed", "filter"):
         K.pca_basis(cov, zsum, n, dims + 1, n_load=dims, ld_l=dims, eigh=method)
         torch.cuda.synchronize()
         st = torch.cuda.current_stream()
@@ -491,10 +492,15 @@ def eigensolver_comparison(K, pipeline, ip, ind, dat, G, feat, n, dims, reps=3):
         qa, _ = np.linalg.qr(a)
         qb, _ = np.linalg.qr(b)
         return float(np.arccos(np.clip(np.linalg.svd(qa.T @ qb, compute_uv=False), -1, 1)).max())
-    a, b = comps["fp64"][0], comps["mixed"][0]
-    out["max_angle_top10_rad"] = angle(a[:, :10], b[:, :10])
-    out["max_angle_all_rad"] = angle(a[:, :dims], b[:, :dims])
-    out["max_eval_rel_diff"] = float(np.max(np.abs(comps["fp64"][1] - comps["mixed"][1]) / np.abs(comps["fp64"][1])))
+        if method == "filter":
+            out["filter_residual"] = K.filter_residual()
+    a = comps["fp64"][0]
+    for method in ("mixed", "filter"):
+        b = comps[method][0]
+        out[f"{method}_max_angle_top10_rad"] = angle(a[:, :10], b[:, :10])
+        out[f"{method}_max_angle_all_rad"] = angle(a[:, :dims], b[:, :dims])
+        out[f"{method}_max_eval_rel_diff"] = float(np.max(np.abs(comps["fp64"][1] - comps[method][1])
+                                                          / np.abs(comps["fp64"][1])))
     return out
 
 

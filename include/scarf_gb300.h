@@ -128,6 +128,27 @@ int sg_pca_basis_mixed(sg_handle* h, const double* cov, const double* zsum, int6
                        int32_t n_cols, int32_t n_comp, double* comps, double* evals, double* evr,
                        int32_t n_load, float* loadings32, int32_t ld_l, void* stream);
 
+/* a4 -- the same outputs as sg_pca_basis from a Chebyshev-filtered block
+ * subspace iteration: FP32 GEMMs apply Chebyshev polynomials of the centred
+ * scatter (damped on [0, cut], cut = the block's smallest Ritz value) to a
+ * block of ~2.5 (n_comp + 16) columns, re-orthonormalised by FP32
+ * Cholesky-QR2 after each segment; an FP32 Rayleigh-Ritz step picks the
+ * n_comp + 16 largest Ritz vectors and the FP64 Rayleigh-Ritz step of
+ * sg_pca_basis_mixed refines them. When a wanted FP64 Ritz pair has a
+ * residual ||A v - w v|| above 1e-4 of the largest eigenvalue, or the matrix
+ * is too small for the block, the result comes from sg_pca_basis_mixed.
+ * Synchronises the stream. No counterpart in the reference beyond the
+ * IncrementalPCA fit it also replaces (scarf/ann.py:207-256). */
+int sg_pca_basis_filter(sg_handle* h, const double* cov, const double* zsum, int64_t n_used,
+                        int32_t n_cols, int32_t n_comp, double* comps, double* evals, double* evr,
+                        int32_t n_load, float* loadings32, int32_t ld_l, void* stream);
+
+/* Max relative FP64 residual of the wanted pairs in the last
+ * sg_pca_basis_filter call on this handle: NaN when the call took the dense
+ * route for a small matrix, infinity when it fell back to it. No counterpart
+ * in the reference. */
+double sg_pca_filter_residual(const sg_handle* h);
+
 /* a5 -- the reducer ((x - mu)/sigma) . L (scarf/ann.py:129-138, :191-192):
  * scores[r*ld_s + c], c < d (columns d..ld_s-1 are written 0). bf16_out (may be
  * NULL) receives a BF16 copy with row stride ld_b (zero padded). */

@@ -272,7 +272,7 @@ class AnnStream:
         cov, zsum = K.covariance(self.data.x, self._mu32, self._sg32, n_cols=self.nFeats, row_mask=mask,
                                  precision=self.precision)
         comps, evals, evr, _ = K.pca_basis(cov, zsum, n_used, self.dims + 1, n_load=self.dims, ld_l=self.dims,
-                                           eigh="mixed" if self.precision == "precision" else "fp64")
+                                           eigh="filter" if self.precision == "precision" else "fp64")
         c = comps.cpu().numpy()
         self._pca = _PcaInfo(c.T, evals.cpu().numpy(), evr.cpu().numpy(), n_used)
         self.loadings = c[:, :-1]

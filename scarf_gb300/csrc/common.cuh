@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <cstddef>
+#include <limits>
 #include <vector>
 
 #include "../../include/scarf_gb300.h"
@@ -21,6 +22,9 @@ struct sg_handle {
   void* blas = nullptr;      // cublasHandle_t, created on first use
   void* solver_work = nullptr;
   size_t solver_work_bytes = 0;
+  // max relative FP64 residual of the last sg_pca_basis_filter call
+  // (NaN: it used the dense route; infinity: it fell back to it)
+  double eig_resid = std::numeric_limits<double>::quiet_NaN();
   // kernel timing (off unless sg_profile(h, 1)): events around named launches
   bool prof = false;
   struct ProfRec {

@@ -12,6 +12,16 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <cmath>
+#include <cstdio>
+
+// SG_EIG_DEBUG (off unless defined at compile time) traces the filtered
+// eigensolver's schedule to stderr.
+#ifdef SG_EIG_DEBUG
+#define EIG_DBG(...) std::fprintf(stderr, __VA_ARGS__)
+#else
+#define EIG_DBG(...) ((void)0)
+#endif
 #include <vector>
 
 int sg_covariance_tc(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld,
@@ -230,6 +240,27 @@ __global__ void basis_kernel(const double* __restrict__ V, const double* __restr
     if (evals) evals[c] = W[src];
     if (evr) evr[c] = W[src] / *trace;
   }
+}
+
+// ||y - w v|| / |w_max| for one Ritz pair per CTA (y = A v)
+__global__ void ritz_residual_kernel(const double* __restrict__ Y, const double* __restrict__ V,
+                                     const double* __restrict__ W, const double* __restrict__ wmax, int n,
+                                     double* __restrict__ out) {
+  __shared__ double red[256];
+  const int c = blockIdx.x;
+  const double w = W[c];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double r = Y[int64_t(c) * n + i] - w * V[int64_t(c) * n + i];
+    s += r * r;
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[c] = sqrt(red[0]) / fabs(*wmax);
 }
 
 __global__ void f64_to_f32_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t ne) {
@@ -459,6 +490,79 @@ int solver_work(sg_handle* h, size_t wbytes) {
 // centred scatter (top n_comp + 16 pairs), then an FP64 Rayleigh-Ritz step on
 // that subspace (FP64 Cholesky-QR orthonormalisation, FP64 Q^T A Q and its
 // FP64 eigendecomposition), so eigenvalues and vectors are FP64 Ritz pairs.
+namespace {
+
+// FP64 Rayleigh-Ritz on the subspace spanned by the m columns of Q (n x m,
+// FP64, overwritten): FP64 Cholesky-QR orthonormalisation, B = Q^T A Q and
+// its FP64 eigendecomposition; V = Q U holds the Ritz vectors and W the Ritz
+// values, both in ascending order. When `resid` is given, it receives
+// max_c ||A v_c - w_c v_c|| / max|w| over the top n_top Ritz pairs (host value;
+// this synchronises the stream).
+int rayleigh_ritz_fp64(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, const double* A, int n, int m,
+                       double* Q, double* Y, double* V, double* G, double* B, double* W, int* info, int lwork_d,
+                       int n_top, double* resid, double* rcol, cudaStream_t st) {
+  const double one = 1.0, zero = 0.0;
+  // Q <- Q R^-1 with Q^T Q = L L^T (R = L^T): FP64 Cholesky-QR
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Q, n, Q, n, &zero, G, m));
+  SG_SOLVER(cusolverDnDpotrf(sol, CUBLAS_FILL_MODE_LOWER, m, G, m, static_cast<double*>(h->solver_work),
+                             int(h->solver_work_bytes / sizeof(double)), info));
+  SG_BLAS(cublasDtrsm(blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, m, &one, G,
+                      m, Q, n));
+  // Rayleigh quotient B = Q^T A Q and its FP64 eigendecomposition
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &one, A, n, Q, n, &zero, Y, n));
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Q, n, Y, n, &zero, B, m));
+  SG_SOLVER(cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, B, m, W,
+                             static_cast<double*>(h->solver_work), lwork_d, info + 1));
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, Q, n, B, m, &zero, V, n));
+  if (resid) {
+    // A V = (A Q) U; the residual of Ritz pair c is (A Q) u_c - w_c v_c
+    SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, Y, n, B, m, &zero, Q, n));
+    ritz_residual_kernel<<<n_top, 256, 0, st>>>(Q + size_t(m - n_top) * n, V + size_t(m - n_top) * n, W + (m - n_top),
+                                                W + (m - 1), n, rcol);
+    SG_LAUNCH_CHECK();
+    std::vector<double> hr(static_cast<size_t>(n_top));
+    SG_CUDA(cudaMemcpyAsync(hr.data(), rcol, sizeof(double) * size_t(n_top), cudaMemcpyDeviceToHost, st));
+    SG_CUDA(cudaStreamSynchronize(st));
+    double mx = 0.0;
+    for (double v : hr) mx = std::isfinite(v) ? std::max(mx, v) : INFINITY;
+    *resid = mx;
+  }
+  return SG_OK;
+}
+
+int check_info(const int* info, int count, cudaStream_t st, const char* what) {
+  std::vector<int> hi(static_cast<size_t>(count));
+  SG_CUDA(cudaMemcpyAsync(hi.data(), info, sizeof(int) * size_t(count), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(cudaStreamSynchronize(st));
+  for (int i = 0; i < count; ++i)
+    if (hi[size_t(i)] != 0) return sg::fail(SG_ERR_CUDA, "%s: factorisation %d info=%d", what, i, hi[size_t(i)]);
+  return SG_OK;
+}
+
+int solver_handles(sg_handle* h, cudaStream_t st, cusolverDnHandle_t* sol, cublasHandle_t* blas) {
+  if (!h->solver) {
+    cusolverDnHandle_t s;
+    SG_SOLVER(cusolverDnCreate(&s));
+    h->solver = s;
+  }
+  if (!h->blas) {
+    cublasHandle_t b;
+    SG_BLAS(cublasCreate(&b));
+    h->blas = b;
+  }
+  *sol = static_cast<cusolverDnHandle_t>(h->solver);
+  *blas = static_cast<cublasHandle_t>(h->blas);
+  SG_SOLVER(cusolverDnSetStream(*sol, st));
+  SG_BLAS(cublasSetStream(*blas, st));
+  return SG_OK;
+}
+
+}  // namespace
+
+// Mixed-precision principal axes: an FP32 partial eigendecomposition of the
+// centred scatter (top n_comp + 16 pairs), then an FP64 Rayleigh-Ritz step on
+// that subspace (FP64 Cholesky-QR orthonormalisation, FP64 Q^T A Q and its
+// FP64 eigendecomposition), so eigenvalues and vectors are FP64 Ritz pairs.
 extern "C" int sg_pca_basis_mixed(sg_handle* h, const double* cov, const double* zsum, int64_t n_used,
                                   int32_t n_cols, int32_t n_comp, double* comps, double* evals, double* evr,
                                   int32_t n_load, float* loadings32, int32_t ld_l, void* stream) {
@@ -470,20 +574,10 @@ extern "C" int sg_pca_basis_mixed(sg_handle* h, const double* cov, const double*
          "sg_pca_basis_mixed: bad loadings shape");
   const int n = n_cols;
   const int m = std::min(n, n_comp + 16);
-  if (!h->solver) {
-    cusolverDnHandle_t s;
-    SG_SOLVER(cusolverDnCreate(&s));
-    h->solver = s;
-  }
-  if (!h->blas) {
-    cublasHandle_t b;
-    SG_BLAS(cublasCreate(&b));
-    h->blas = b;
-  }
-  cusolverDnHandle_t sol = static_cast<cusolverDnHandle_t>(h->solver);
-  cublasHandle_t blas = static_cast<cublasHandle_t>(h->blas);
-  SG_SOLVER(cusolverDnSetStream(sol, st));
-  SG_BLAS(cublasSetStream(blas, st));
+  cusolverDnHandle_t sol;
+  cublasHandle_t blas;
+  int rc = solver_handles(h, st, &sol, &blas);
+  if (rc) return rc;
   const size_t nn = size_t(n) * n, nm = size_t(n) * m, mm = size_t(m) * m;
   const size_t need = sg::Carver::need(nn * 8) + sg::Carver::need(nn * 4) + 3 * sg::Carver::need(nm * 8) +
                       2 * sg::Carver::need(mm * 8) + 2 * sg::Carver::need(size_t(n) * 8) + 1024;
@@ -501,7 +595,7 @@ extern "C" int sg_pca_basis_mixed(sg_handle* h, const double* cov, const double*
   float* W32 = cv.take<float>(n);
   double* W = cv.take<double>(n);
   double* tr = cv.take<double>(1);
-  int* info = cv.take<int>(1);
+  int* info = cv.take<int>(4);
   const int64_t ne = int64_t(nn);
   center_kernel<<<sg::ceil_div_i(ne, 256), 256, 0, st>>>(cov, zsum, 1.0 / double(n_used), n, A);
   SG_LAUNCH_CHECK();
@@ -517,32 +611,395 @@ extern "C" int sg_pca_basis_mixed(sg_handle* h, const double* cov, const double*
   int lwork_d = 0;
   SG_SOLVER(cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, B, m, W, &lwork_d));
   const size_t wb = std::max(sizeof(float) * size_t(lwork), sizeof(double) * size_t(lwork_d));
-  int rc = solver_work(h, wb);
+  rc = solver_work(h, wb);
   if (rc) return rc;
   SG_SOLVER(cusolverDnSsyevdx(sol, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER, n, A32, n,
-                              0.f, 0.f, il, iu, &meig, W32, static_cast<float*>(h->solver_work), lwork, info));
+                              0.f, 0.f, il, iu, &meig, W32, static_cast<float*>(h->solver_work), lwork, info + 2));
   if (meig != m) return sg::fail(SG_ERR_CUDA, "cusolverDnSsyevdx returned %d of %d eigenpairs", meig, m);
   f32_to_f64_kernel<<<sg::ceil_div_i(int64_t(nm), 256), 256, 0, st>>>(A32, Q, int64_t(nm));
   SG_LAUNCH_CHECK();
-  const double one = 1.0, zero = 0.0;
-  // Q <- Q R^-1 with Q^T Q = L L^T (R = L^T): FP64 Cholesky-QR
-  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Q, n, Q, n, &zero, G, m));
-  SG_SOLVER(cusolverDnDpotrf(sol, CUBLAS_FILL_MODE_LOWER, m, G, m, static_cast<double*>(h->solver_work),
-                             int(h->solver_work_bytes / sizeof(double)), info));
-  SG_BLAS(cublasDtrsm(blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, m, &one, G,
-                      m, Q, n));
-  // Rayleigh quotient B = Q^T A Q and its FP64 eigendecomposition
-  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &one, A, n, Q, n, &zero, Y, n));
-  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Q, n, Y, n, &zero, B, m));
-  SG_SOLVER(cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, B, m, W,
-                             static_cast<double*>(h->solver_work), lwork_d, info));
-  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, Q, n, B, m, &zero, V, n));
-  int hinfo = 0;
-  SG_CUDA(cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st));
-  SG_CUDA(cudaStreamSynchronize(st));
-  if (hinfo != 0) return sg::fail(SG_ERR_CUDA, "sg_pca_basis_mixed: factorisation info=%d", hinfo);
+  rc = rayleigh_ritz_fp64(h, sol, blas, A, n, m, Q, Y, V, G, B, W, info, lwork_d, n_comp, nullptr, nullptr, st);
+  if (rc) return rc;
+  rc = check_info(info, 3, st, "sg_pca_basis_mixed");
+  if (rc) return rc;
   // the n_comp largest Ritz pairs are the last n_comp columns (ascending order)
   basis_kernel<<<n_comp, 256, 0, st>>>(V + size_t(m - n_comp) * n, W + (m - n_comp), n, n_comp, tr, comps, evals,
+                                       evr, n_load, loadings32, ld_l);
+  SG_LAUNCH_CHECK();
+  SG_CUDA(cudaStreamSynchronize(st));
+  return SG_OK;
+}
+
+namespace {
+
+// uniform(-1, 1) block from a counter hash (the SplitMix64 finaliser)
+__global__ void random_block_kernel(float* __restrict__ X, int64_t ne, uint64_t seed) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  uint64_t z = uint64_t(e) * 0x9E3779B97F4A7C15ull + seed;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  X[e] = float(int32_t(uint32_t(z >> 32))) * (1.0f / 2147483648.0f);
+}
+
+// largest absolute row sum (an upper bound of the spectral radius)
+__global__ void absrow_max_kernel(const float* __restrict__ A, int n, float* __restrict__ out) {
+  __shared__ float red[256];
+  float mx = 0.f;
+  for (int i = blockIdx.x; i < n; i += gridDim.x) {
+    float s = 0.f;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) s += fabsf(A[int64_t(i) * n + j]);
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+      if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+      __syncthreads();
+    }
+    mx = fmaxf(mx, red[0]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicMax(reinterpret_cast<int*>(out), __float_as_int(mx));  // non-negative floats
+}
+
+// Column scaling for Cholesky-QR: with d = diag(Y^T Y), G <- D G D and
+// Y <- Y D for D = diag(d)^(-1/2), so the Gram matrix has a unit diagonal (a
+// non-positive d_j leaves column j unscaled; the factorisation then fails).
+__global__ void gram_scale_kernel(float* __restrict__ G, const float* __restrict__ diag, int m) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= int64_t(m) * m) return;
+  const int i = int(e % m), j = int(e / m);
+  const float di = diag[i], dj = diag[j];
+  G[e] *= (di > 0.f ? rsqrtf(di) : 1.f) * (dj > 0.f ? rsqrtf(dj) : 1.f);
+}
+
+__global__ void diag_copy_kernel(const float* __restrict__ G, float* __restrict__ diag, int m) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < m) diag[j] = G[int64_t(j) * m + j];
+}
+
+__global__ void col_rscale_kernel(float* __restrict__ Y, const float* __restrict__ diag, int n, int m) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= int64_t(n) * m) return;
+  const float g = diag[e / n];
+  Y[e] *= g > 0.f ? rsqrtf(g) : 1.f;
+}
+
+// Rayleigh quotients of the block's last K columns from the first filter
+// product C = a1 A X - X: x^T A x = (x^T c + x^T x) / a1
+__global__ void tail_rq_kernel(const float* __restrict__ X, const float* __restrict__ C, int n, int m, int K, float a1,
+                               float* __restrict__ out) {
+  __shared__ float red[2][256];
+  const int j = m - K + blockIdx.x;
+  float s = 0.f, q = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float x = X[int64_t(j) * n + i];
+    s = fmaf(x, C[int64_t(j) * n + i], s);
+    q = fmaf(x, x, q);
+  }
+  red[0][threadIdx.x] = s;
+  red[1][threadIdx.x] = q;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + o];
+      red[1][threadIdx.x] += red[1][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = (red[0][0] + red[1][0]) / (a1 * red[1][0]);
+}
+
+// reverse the column order of an m x m column-major matrix
+__global__ void reverse_cols_kernel(float* __restrict__ G, int m) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int half = m / 2;
+  if (e >= int64_t(half) * m) return;
+  const int j = int(e / m), i = int(e % m);
+  const int64_t a = int64_t(j) * m + i, b = int64_t(m - 1 - j) * m + i;
+  const float t = G[a];
+  G[a] = G[b];
+  G[b] = t;
+}
+
+struct FilterBufs {
+  float* X;   // n x m, orthonormal block
+  float* P;   // n x m scratch
+  float* Q;   // n x m scratch
+  float* G;   // m x m
+  float* W;   // m Ritz values
+  float* D;   // m diagonal of the Gram matrix
+  float* R;   // Rayleigh quotients of the last columns
+  int* info;  // one slot per factorisation
+  int n_info;
+  int cap_info;
+};
+
+// Y <- Y D L^-T with (Y D)^T (Y D) = L L^T and D the column scaling, twice
+// (FP32 Cholesky-QR2 on unit-norm columns). The first columns keep their
+// span: the block stays ordered with its dominant directions first.
+int cholqr2_f32(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, float* Y, int n, int m, FilterBufs& b,
+                cudaStream_t st) {
+  const float one = 1.f, zero = 0.f;
+  for (int pass = 0; pass < 2; ++pass) {
+    SG_BLAS(cublasSgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Y, n, Y, n, &zero, b.G, m));
+    diag_copy_kernel<<<sg::ceil_div_i(m, 256), 256, 0, st>>>(b.G, b.D, m);
+    SG_LAUNCH_CHECK();
+    gram_scale_kernel<<<sg::ceil_div_i(int64_t(m) * m, 256), 256, 0, st>>>(b.G, b.D, m);
+    SG_LAUNCH_CHECK();
+    col_rscale_kernel<<<sg::ceil_div_i(int64_t(n) * m, 256), 256, 0, st>>>(Y, b.D, n, m);
+    SG_LAUNCH_CHECK();
+    int* inf = b.info + std::min(b.n_info, b.cap_info - 1);
+    ++b.n_info;
+    SG_SOLVER(cusolverDnSpotrf(sol, CUBLAS_FILL_MODE_LOWER, m, b.G, m, static_cast<float*>(h->solver_work),
+                               int(h->solver_work_bytes / sizeof(float)), inf));
+    SG_BLAS(cublasStrsm(blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, m, &one,
+                        b.G, m, Y, n));
+  }
+  return SG_OK;
+}
+
+constexpr int kTailCols = 8;
+
+// One filter segment on the block X: X <- orth(T_deg((2A - cut I)/cut) X),
+// the Chebyshev polynomial that is bounded by 1 on [0, cut] and grows fastest
+// above it. Recurrence: Y1 = (2/cut) A X - X, Y_{k+1} = (4/cut) A Y_k - 2 Y_k - Y_{k-1}.
+// *tail_rq receives the smallest Rayleigh quotient of the input block's last
+// kTailCols columns (host value; synchronises).
+int filter_segment(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, const float* A32, int n, int m, int deg,
+                   double cut, FilterBufs& b, cudaStream_t st, float* tail_rq) {
+  const float a1 = float(2.0 / cut), a2 = float(4.0 / cut), m1 = -1.f, m2 = -2.f, one = 1.f;
+  float* prev = b.X;
+  float* cur = b.P;
+  SG_CUDA(cudaMemcpyAsync(cur, prev, sizeof(float) * size_t(n) * m, cudaMemcpyDeviceToDevice, st));
+  SG_BLAS(cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &a1, A32, n, prev, n, &m1, cur, n));
+  const int K = std::min(kTailCols, m);
+  tail_rq_kernel<<<K, 256, 0, st>>>(prev, cur, n, m, K, a1, b.R);
+  SG_LAUNCH_CHECK();
+  float hr[kTailCols];
+  SG_CUDA(cudaMemcpyAsync(hr, b.R, sizeof(float) * size_t(K), cudaMemcpyDeviceToHost, st));
+  for (int k = 2; k <= deg; ++k) {
+    // prev <- -prev - 2 cur, then prev <- (4/cut) A cur + prev
+    SG_BLAS(cublasSgeam(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, &m1, prev, n, &m2, cur, n, prev, n));
+    SG_BLAS(cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &a2, A32, n, cur, n, &one, prev, n));
+    std::swap(prev, cur);
+  }
+  int rc = cholqr2_f32(h, sol, blas, cur, n, m, b, st);
+  if (rc) return rc;
+  SG_CUDA(cudaStreamSynchronize(st));
+  float mn = INFINITY;
+  for (int k = 0; k < K; ++k) mn = std::isfinite(hr[k]) ? std::min(mn, hr[k]) : mn;
+  *tail_rq = mn;
+  if (cur != b.X) {
+    // keep X as the block; the other two buffers stay scratch
+    if (cur == b.P) std::swap(b.X, b.P);
+    else std::swap(b.X, b.Q);
+  }
+  return SG_OK;
+}
+
+// FP32 Rayleigh-Ritz of the block: X <- X U (Ritz vectors, descending: the
+// dominant directions first); the Ritz values, ascending, are copied to `wh`
+// (host, synchronising).
+int ritz_f32(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, const float* A32, int n, int m, FilterBufs& b,
+             int lwork_s, std::vector<float>& wh, bool vectors, cudaStream_t st) {
+  const float one = 1.f, zero = 0.f;
+  SG_BLAS(cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &one, A32, n, b.X, n, &zero, b.P, n));
+  SG_BLAS(cublasSgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, b.X, n, b.P, n, &zero, b.G, m));
+  int* inf = b.info + std::min(b.n_info, b.cap_info - 1);
+  ++b.n_info;
+  SG_SOLVER(cusolverDnSsyevd(sol, vectors ? CUSOLVER_EIG_MODE_VECTOR : CUSOLVER_EIG_MODE_NOVECTOR,
+                             CUBLAS_FILL_MODE_LOWER, m, b.G, m, b.W, static_cast<float*>(h->solver_work), lwork_s, inf));
+  if (vectors) {
+    reverse_cols_kernel<<<sg::ceil_div_i(int64_t(m / 2) * m, 256), 256, 0, st>>>(b.G, m);
+    SG_LAUNCH_CHECK();
+    SG_BLAS(cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, b.X, n, b.G, m, &zero, b.P, n));
+    std::swap(b.X, b.P);
+  }
+  wh.resize(size_t(m));
+  SG_CUDA(cudaMemcpyAsync(wh.data(), b.W, sizeof(float) * size_t(m), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(cudaStreamSynchronize(st));
+  return SG_OK;
+}
+
+// degree s of the largest s <= smax with T_s(t) <= bound (t >= 1)
+int cheb_degree(double t, double bound, int smax) {
+  int s = 1;
+  for (int k = 2; k <= smax; ++k) {
+    if (std::cosh(k * std::acosh(std::max(1.0, t))) > bound) break;
+    s = k;
+  }
+  return s;
+}
+
+}  // namespace
+
+// Principal axes by Chebyshev-filtered block subspace iteration: FP32 cuBLAS
+// GEMMs apply Chebyshev polynomials of the centred scatter, damped on [0, cut]
+// (cut = the smallest Ritz value of the block, which never exceeds the
+// block's m-th eigenvalue, so no wanted pair is damped), to an m-wide block
+// that is re-orthonormalised (FP32 Cholesky-QR2) after each segment. An FP32
+// Rayleigh-Ritz step picks the top n_comp + 16 Ritz vectors and the FP64
+// Rayleigh-Ritz step of the mixed solver refines them. If the FP64 residual
+// of a wanted pair exceeds 1e-4 of the largest eigenvalue, or the problem is
+// too small for the block, the mixed solver runs instead.
+extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double* zsum, int64_t n_used,
+                                   int32_t n_cols, int32_t n_comp, double* comps, double* evals, double* evr,
+                                   int32_t n_load, float* loadings32, int32_t ld_l, void* stream) {
+  SG_HANDLE_CHECK(h);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  SG_ARG(cov && comps && n_cols > 0 && n_used > 0, "sg_pca_basis_filter: bad arguments");
+  SG_ARG(n_comp >= 1 && n_comp <= n_cols, "sg_pca_basis_filter: n_comp=%d outside [1, %d]", n_comp, n_cols);
+  SG_ARG(!loadings32 || (n_load >= 0 && n_load <= n_comp && ld_l >= n_load),
+         "sg_pca_basis_filter: bad loadings shape");
+  const int n = n_cols;
+  const int p = n_comp + 16;
+  const int m = int(sg::ceil_div(std::max<int64_t>(p + 64, (5 * int64_t(p)) / 2), 32) * 32);
+  h->eig_resid = NAN;
+  if (m > 256 || 2 * m > n || n_used < 4 * int64_t(m))
+    return sg_pca_basis_mixed(h, cov, zsum, n_used, n_cols, n_comp, comps, evals, evr, n_load, loadings32, ld_l,
+                              stream);
+  cusolverDnHandle_t sol;
+  cublasHandle_t blas;
+  int rc = solver_handles(h, st, &sol, &blas);
+  if (rc) return rc;
+  const size_t nn = size_t(n) * n, nm = size_t(n) * m, np = size_t(n) * p, pp = size_t(p) * p;
+  const int cap_info = 128;
+  const size_t need = sg::Carver::need(nn * 8) + sg::Carver::need(nn * 4) + 3 * sg::Carver::need(nm * 4) +
+                      sg::Carver::need(size_t(m) * m * 4) + 2 * sg::Carver::need(size_t(m) * 4) +
+                      sg::Carver::need(kTailCols * 4) +
+                      3 * sg::Carver::need(np * 8) + 2 * sg::Carver::need(pp * 8) + sg::Carver::need(size_t(p) * 8) +
+                      sg::Carver::need(size_t(p) * 8) + sg::Carver::need(16) + sg::Carver::need(cap_info * 4);
+  int status;
+  void* w = sg::ws_get(h, need, &status);
+  if (!w) return status;
+  sg::Carver cv(w);
+  double* A = cv.take<double>(nn);
+  float* A32 = cv.take<float>(nn);
+  FilterBufs b;
+  b.X = cv.take<float>(nm);
+  b.P = cv.take<float>(nm);
+  b.Q = cv.take<float>(nm);
+  b.G = cv.take<float>(size_t(m) * m);
+  b.W = cv.take<float>(size_t(m));
+  b.D = cv.take<float>(size_t(m));
+  b.R = cv.take<float>(size_t(kTailCols));
+  double* Qd = cv.take<double>(np);
+  double* Yd = cv.take<double>(np);
+  double* Vd = cv.take<double>(np);
+  double* Gd = cv.take<double>(pp);
+  double* Bd = cv.take<double>(pp);
+  double* Wd = cv.take<double>(size_t(p));
+  double* rcol = cv.take<double>(size_t(p));
+  double* tr = cv.take<double>(2);
+  b.info = cv.take<int>(cap_info);
+  b.n_info = 0;
+  b.cap_info = cap_info;
+  SG_CUDA(cudaMemsetAsync(b.info, 0, sizeof(int) * cap_info, st));
+  const int64_t ne = int64_t(nn);
+  center_kernel<<<sg::ceil_div_i(ne, 256), 256, 0, st>>>(cov, zsum, 1.0 / double(n_used), n, A);
+  SG_LAUNCH_CHECK();
+  trace_kernel<<<1, 256, 0, st>>>(A, n, tr);
+  SG_LAUNCH_CHECK();
+  f64_to_f32_kernel<<<sg::ceil_div_i(ne, 256), 256, 0, st>>>(A, A32, ne);
+  SG_LAUNCH_CHECK();
+  sg::ProfScope prof(h, "eigh", st);
+  float* rowmax = reinterpret_cast<float*>(tr + 1);
+  SG_CUDA(cudaMemsetAsync(rowmax, 0, sizeof(float), st));
+  absrow_max_kernel<<<std::min(n, 4 * h->sm_count), 256, 0, st>>>(A32, n, rowmax);
+  SG_LAUNCH_CHECK();
+  random_block_kernel<<<sg::ceil_div_i(int64_t(nm), 256), 256, 0, st>>>(b.X, int64_t(nm), 0x5CA2F00Dull);
+  SG_LAUNCH_CHECK();
+  // workspace: FP32 potrf / syevd of m, FP64 potrf / syevd of p
+  int lw_potrf = 0, lw_s = 0, lw_d = 0, lw_dp = 0;
+  SG_SOLVER(cusolverDnSpotrf_bufferSize(sol, CUBLAS_FILL_MODE_LOWER, m, b.G, m, &lw_potrf));
+  SG_SOLVER(cusolverDnSsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, b.G, m, b.W, &lw_s));
+  SG_SOLVER(cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, p, Bd, p, Wd, &lw_d));
+  SG_SOLVER(cusolverDnDpotrf_bufferSize(sol, CUBLAS_FILL_MODE_LOWER, p, Gd, p, &lw_dp));
+  const size_t wb = std::max(std::max(sizeof(float) * size_t(lw_potrf), sizeof(float) * size_t(lw_s)),
+                             std::max(sizeof(double) * size_t(lw_d), sizeof(double) * size_t(lw_dp)));
+  rc = solver_work(h, wb);
+  if (rc) return rc;
+  rc = cholqr2_f32(h, sol, blas, b.X, n, m, b, st);
+  if (rc) return rc;
+  double hd[2];
+  SG_CUDA(cudaMemcpyAsync(hd, tr, sizeof(double), cudaMemcpyDeviceToHost, st));
+  float hrow = 0.f;
+  SG_CUDA(cudaMemcpyAsync(&hrow, rowmax, sizeof(float), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(cudaStreamSynchronize(st));
+  const double trace = hd[0];
+  // phase A: the mean eigenvalue as the cut, degrees bounded by the row-sum bound
+  double cut = std::max(trace / n, 1e-30);
+  int deg = cheb_degree(2.0 * double(hrow) / cut - 1.0, 1e3, 8);
+  EIG_DBG("filter: n=%d m=%d p=%d trace/n=%g rowmax=%g degA=%d\n", n, m, p, cut, double(hrow), deg);
+  float rq = 0.f;
+  for (int s = 0; s < 2; ++s) {
+    rc = filter_segment(h, sol, blas, A32, n, m, deg, cut, b, st, &rq);
+    if (rc) return rc;
+  }
+  // phase B: cut from the block's smallest Ritz value, degree from its largest
+  std::vector<float> th;
+  rc = ritz_f32(h, sol, blas, A32, n, m, b, lw_s, th, true, st);
+  if (rc) return rc;
+  bool ok = th[0] > 0.f && std::isfinite(th[size_t(m - 1)]);
+  EIG_DBG("filter: RR1 ok=%d theta_min=%g theta_max=%g\n", int(ok), double(th[0]), double(th[size_t(m - 1)]));
+  double resid = INFINITY;
+  if (ok) {
+    // The cut starts at the block's smallest Ritz value (never above its
+    // m-th eigenvalue) and rises with the smallest Rayleigh quotient of the
+    // block's last columns as the block converges, capped at 0.99 x the Ritz
+    // value of pair n_comp + 8, which is a lower bound of that eigenvalue: no
+    // wanted pair is ever damped.
+    cut = double(th[0]);
+    const double theta_w = double(th[size_t(m - std::min(m, n_comp + 8))]);
+    const double cut_cap = 0.99 * theta_w;
+    const double theta_max = 1.05 * double(th[size_t(m - 1)]);
+    const double t_w = 2.0 * theta_w / cut - 1.0;
+    const double rate = t_w > 1.0 ? std::acosh(t_w) : 0.0;
+    int total = rate > 0.0 ? int(std::ceil(std::log(1e10) / rate)) : 240;
+    total = std::min(240, std::max(total, 8));
+    // long segments while the dominant directions lead the block (their
+    // growth over the weakest column at most 1e5), then two short ones
+    // (growth at most 1e2) that leave the block accurate to FP32
+    int done = 0, segs = 0;
+    EIG_DBG("filter: RR1 theta_min=%g theta_w=%g theta_max=%g t_w=%g total=%d\n", double(th[0]), theta_w,
+            double(th[size_t(m - 1)]), t_w, total);
+    for (int polish = 0; done < total || polish < 2; ++segs) {
+      const double t_max = 2.0 * theta_max / cut - 1.0;
+      const bool last = done >= total;
+      const int d = cheb_degree(t_max, last ? 1e2 : 1e5, 8);
+      rc = filter_segment(h, sol, blas, A32, n, m, d, cut, b, st, &rq);
+      if (rc) return rc;
+      EIG_DBG("filter: seg %d deg %d cut %g tail_rq %g\n", segs, d, cut, double(rq));
+      if (std::isfinite(rq)) cut = std::min(cut_cap, std::max(cut, double(rq)));
+      if (last) ++polish;
+      else done += d;
+      if (segs > 120) break;
+    }
+    rc = ritz_f32(h, sol, blas, A32, n, m, b, lw_s, th, true, st);
+    if (rc) return rc;
+    // the top p Ritz vectors (the first p columns) -> FP64 Rayleigh-Ritz with a residual check
+    f32_to_f64_kernel<<<sg::ceil_div_i(int64_t(np), 256), 256, 0, st>>>(b.X, Qd, int64_t(np));
+    SG_LAUNCH_CHECK();
+    rc = rayleigh_ritz_fp64(h, sol, blas, A, n, p, Qd, Yd, Vd, Gd, Bd, Wd, b.info + cap_info - 2, lw_d, n_comp,
+                            &resid, rcol, st);
+    if (rc) return rc;
+    std::vector<int> hi(static_cast<size_t>(cap_info));
+    SG_CUDA(cudaMemcpyAsync(hi.data(), b.info, sizeof(int) * cap_info, cudaMemcpyDeviceToHost, st));
+    SG_CUDA(cudaStreamSynchronize(st));
+    for (int i = 0; i < cap_info; ++i)
+      if (hi[size_t(i)] != 0) {
+        EIG_DBG("filter: factorisation slot %d info=%d (of %d used)\n", i, hi[size_t(i)], b.n_info);
+        ok = false;
+      }
+    EIG_DBG("filter: RR2 theta_min=%g theta_max=%g resid=%g\n", double(th[0]), double(th[size_t(m - 1)]), resid);
+    ok = ok && b.n_info < cap_info - 2 && resid <= 1e-4;
+  }
+  h->eig_resid = ok ? resid : INFINITY;
+  if (!ok)
+    return sg_pca_basis_mixed(h, cov, zsum, n_used, n_cols, n_comp, comps, evals, evr, n_load, loadings32, ld_l,
+                              stream);
+  basis_kernel<<<n_comp, 256, 0, st>>>(Vd + size_t(p - n_comp) * n, Wd + (p - n_comp), n, n_comp, tr, comps, evals,
                                        evr, n_load, loadings32, ld_l);
   SG_LAUNCH_CHECK();
   SG_CUDA(cudaStreamSynchronize(st));
@@ -574,3 +1031,5 @@ extern "C" int sg_project(sg_handle* h, const float* x, int64_t n_rows, int32_t 
   }
   return SG_OK;
 }
+
+extern "C" double sg_pca_filter_residual(const sg_handle* h) { return h ? h->eig_resid : NAN; }

@@ -169,7 +169,9 @@ def pca_basis(cov: torch.Tensor, zsum: Optional[torch.Tensor], n_used: int, n_co
               n_load: Optional[int] = None, ld_l: Optional[int] = None, eigh: str = "fp64"):
     """a4: top ``n_comp`` principal axes on the device, svd_flip signs.
     ``eigh='fp64'``: FP64 partial eigendecomposition of the whole scatter;
-    ``eigh='mixed'``: FP32 partial eigendecomposition + FP64 Rayleigh-Ritz.
+    ``eigh='mixed'``: FP32 partial eigendecomposition + FP64 Rayleigh-Ritz;
+    ``eigh='filter'``: Chebyshev-filtered FP32 subspace iteration + FP64
+    Rayleigh-Ritz (see ``filter_residual``).
 
     Returns ``(comps h x n_comp f64, evals, evr, loadings32 h x ld_l)`` where
     loadings32 holds the first ``n_load`` (default n_comp - 1) components."""
@@ -182,10 +184,18 @@ def pca_basis(cov: torch.Tensor, zsum: Optional[torch.Tensor], n_used: int, n_co
     evals = torch.empty(n_comp, dtype=torch.float64, device=dev)
     evr = torch.empty(n_comp, dtype=torch.float64, device=dev)
     l32 = torch.empty((h, ld_l), dtype=torch.float32, device=dev)
-    fn = {"fp64": L.load().sg_pca_basis, "mixed": L.load().sg_pca_basis_mixed}[eigh]
+    fn = {"fp64": L.load().sg_pca_basis, "mixed": L.load().sg_pca_basis_mixed,
+          "filter": L.load().sg_pca_basis_filter}[eigh]
     L.check(fn(handle(dev.index).ptr, _p(cov), _p(zsum), int(n_used), h, n_comp, _p(comps), _p(evals), _p(evr),
                n_load, _p(l32), ld_l, _stream(dev)))
     return comps, evals, evr, l32
+
+
+def filter_residual(device: Optional[int] = None) -> float:
+    """Max relative FP64 residual of the wanted pairs of the last
+    ``pca_basis(eigh='filter')`` on this thread's handle (NaN: dense route for
+    a small matrix; inf: fell back to the mixed solver)."""
+    return float(L.load().sg_pca_filter_residual(handle(device).ptr))
 
 
 def project(x: torch.Tensor, mu32, sigma32, loadings32: torch.Tensor, d: int, n_cols: Optional[int] = None,

@@ -149,9 +149,9 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k:
 
     ``precision`` selects the form: "plain" (FP32 scatter, FP32 kNN, full FP64
     eigendecomposition) or "precision" (3xBF16 scatter, BF16 tcgen05 kNN with
-    FP32 re-rank, FP32 partial eigendecomposition refined by an FP64
-    Rayleigh-Ritz step). ``cov_form`` and ``eigh`` override the scatter form
-    and the eigensolver ("fp64" or "mixed")."""
+    FP32 re-rank, Chebyshev-filtered FP32 subspace iteration refined by an
+    FP64 Rayleigh-Ritz step). ``cov_form`` and ``eigh`` override the scatter
+    form and the eigensolver ("fp64", "mixed" or "filter")."""
     dev = torch.device(device)
     n = len(indptr) - 1
     h = len(feat_idx)
@@ -171,7 +171,7 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k:
         cov_form = precision if precision in COV_FORMS else "plain"
     cov, zsum = K.covariance(x, mu32, sigma32, n_cols=h, row_mask=mask, precision=cov_form)
     if eigh is None:
-        eigh = "mixed" if precision == "precision" else "fp64"
+        eigh = "filter" if precision == "precision" else "fp64"
     comps, evals, evr, l32 = K.pca_basis(cov, zsum, n_used, dims + 1, n_load=dims, ld_l=dims, eigh=eigh)
     scores = K.project(x, mu32, sigma32, l32, dims, n_cols=h)
     if margin is None:

@@ -13,7 +13,7 @@ HEADER = os.path.join(ROOT, "include", "scarf_gb300.h")
 
 def declared():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*|size_t|unsigned long long)\s+(sg_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*|size_t|unsigned long long|double)\s+(sg_\w+)\s*\(", text, re.M)))
 
 
 @pytest.fixture(scope="module")

@@ -179,6 +179,50 @@ def test_covariance_long_accumulation(K):
     assert err["plain"] <= 1.2e-4
 
 
+def _spiked_cov(h, n_cells, n_spikes, seed):
+    # Z^T Z of n_cells rows: n_spikes strong directions over a Marchenko-Pastur bulk
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    z = torch.randn((n_cells, h), generator=g, device="cuda", dtype=torch.float64)
+    idx = torch.randperm(h, generator=g, device="cuda")[:n_spikes]
+    scale = torch.linspace(4.0, 1.3, n_spikes, device="cuda", dtype=torch.float64)
+    z[:, idx] *= scale[None, :]
+    return z.T @ z, z.sum(0)
+
+
+@pytest.mark.parametrize("h,n_cells,n_comp", [(2000, 40_000, 51), (1200, 20_000, 31)])
+def test_pca_basis_filter_matches_fp64(K, h, n_cells, n_comp):
+    # 18 spikes over a Marchenko-Pastur bulk: components 19.. sit in the bulk,
+    # where the FP32 rounding of the scatter alone moves single eigenvectors
+    # by ~1e-4 rad; the FP64 Rayleigh-Ritz step keeps the eigenvalues to
+    # second order in that error
+    cov, zsum = _spiked_cov(h, n_cells, 18, seed=h)
+    a = K.pca_basis(cov, zsum, n_cells, n_comp, n_load=n_comp - 1, ld_l=n_comp - 1)
+    b = K.pca_basis(cov, zsum, n_cells, n_comp, n_load=n_comp - 1, ld_l=n_comp - 1, eigh="filter")
+    r = K.filter_residual()
+    ca, cb = a[0].cpu().numpy(), b[0].cpu().numpy()
+    ea, eb = a[1].cpu().numpy(), b[1].cpu().numpy()
+    ang = oracle.subspace_angles(ca[:, :n_comp - 1], cb[:, :n_comp - 1]).max()
+    ang18 = oracle.subspace_angles(ca[:, :18], cb[:, :18]).max()
+    ev = np.abs(ea - eb).max() / np.abs(ea).max()
+    spike = np.abs(ca[:, :5] - cb[:, :5]).max()
+    print(f"filter residual {r:.2e}, angle all {ang:.2e}, spikes {ang18:.2e}, evals {ev:.2e}, top-5 {spike:.2e}")
+    assert np.isfinite(r) and r <= 1e-4           # the filtered route ran and converged
+    assert ang < 5e-4 and ang18 < 1e-5
+    assert ev < 1e-8
+    assert spike < 1e-5                            # separated spikes agree one by one, signs included
+    assert np.allclose(a[2].cpu().numpy(), b[2].cpu().numpy(), rtol=1e-7)
+
+
+def test_pca_basis_filter_small_matrix_takes_dense_route(K, counts):
+    x, cs, cq, _ = _normalize(K, counts)
+    mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
+    cov, zsum = K.covariance(x, mu32, sg32, n_cols=len(counts[4]))
+    b = K.pca_basis(cov, zsum, x.shape[0], 120, n_load=119, ld_l=119, eigh="filter")
+    assert np.isnan(K.filter_residual())           # block wider than half the matrix
+    a = K.pca_basis(cov, zsum, x.shape[0], 120, n_load=119, ld_l=119, eigh="mixed")
+    assert np.array_equal(a[0].cpu().numpy(), b[0].cpu().numpy())
+
+
 def test_pca_basis_mixed_matches_fp64(K, counts):
     x, cs, cq, _ = _normalize(K, counts)
     mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
