@@ -137,12 +137,17 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
 
 
+# DRAM bytes (read + write) per launch from one ncu capture of the full-size
+# C2 step (dram__bytes_read.sum + dram__bytes_write.sum, one pass; the command
+# and the per-kernel table are in profiles/dram_traffic_make_graph_c2.md)
+DRAM_TRAFFIC = {
+    "c2:normalize": 2_633_393_493, "c2:zsplit": 1_596_762_880, "c2:cov_tc": 1_668_659_200,
+    "c2:project": 819_488_939, "c2:knn_tc": 25_846_699, "c2:rerank": 54_053_632, "c2:smooth": 93_588_053,
+}
+
+
 def traffic_table():
-    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f)
-    return {}
+    return DRAM_TRAFFIC
 
 
 def kernel_work(cfg, nnz):

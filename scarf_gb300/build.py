@@ -1,6 +1,6 @@
 """Build recipe of the scarf_gb300 CUDA library (sm_103a).
 
-Every ``csrc/*.cu`` is compiled by nvcc in parallel into ``_build/`` and
+Every ``csrc/*.cu`` (and host-only ``csrc/*.cpp``) is compiled by nvcc in parallel into ``_build/`` and
 linked into ``_build/libscarfgpu.so``. The library is loaded in-tree by
 ``scarf_gb300._lib``; nothing is installed.
 """
@@ -48,6 +48,8 @@ def _flags(verbose_ptx: bool = False):
 def _compile(src: Path, verbose_ptx: bool) -> tuple[Path, str]:
     obj = OUT / (src.stem + ".o")
     cmd = [nvcc(), "-c", str(src), "-o", str(obj)] + _flags(verbose_ptx)
+    if src.suffix == ".cpp":  # host code: the same arithmetic on x86 and Arm hosts
+        cmd += ["-Xcompiler", "-ffp-contract=off"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")
@@ -58,7 +60,8 @@ def up_to_date() -> bool:
     if not LIB.exists():
         return False
     t = LIB.stat().st_mtime
-    deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list((HERE.parent / "include").glob("*.h"))
+    deps = (list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h"))
+            + list((HERE.parent / "include").glob("*.h")))
     deps.append(Path(__file__))
     return all(p.stat().st_mtime <= t for p in deps)
 
@@ -67,7 +70,7 @@ def build(force: bool = False, verbose_ptx: bool = False, quiet: bool = True) ->
     if not force and up_to_date():
         return LIB
     OUT.mkdir(exist_ok=True)
-    srcs = sorted(CSRC.glob("*.cu"))
+    srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
     logs = []
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         for obj, log in ex.map(lambda s: _compile(s, verbose_ptx), srcs):

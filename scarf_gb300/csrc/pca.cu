@@ -7,6 +7,7 @@
 // reduced in FP64 in a fixed order. The z-transform (and the PCA row mask) is
 // applied while staging each 16-row slab into shared memory.
 #include "common.cuh"
+#include "symeig.h"
 
 #include <cublas_v2.h>
 #include <cusolverDn.h>
@@ -508,11 +509,22 @@ int rayleigh_ritz_fp64(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas
                              int(h->solver_work_bytes / sizeof(double)), info));
   SG_BLAS(cublasDtrsm(blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, m, &one, G,
                       m, Q, n));
-  // Rayleigh quotient B = Q^T A Q and its FP64 eigendecomposition
+  // Rayleigh quotient B = Q^T A Q and its FP64 eigendecomposition, on the
+  // host: at these sizes a device solver is bound by launch latency
   SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &one, A, n, Q, n, &zero, Y, n));
   SG_BLAS(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Q, n, Y, n, &zero, B, m));
-  SG_SOLVER(cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, B, m, W,
-                             static_cast<double*>(h->solver_work), lwork_d, info + 1));
+  {
+    const size_t mm = static_cast<size_t>(m) * static_cast<size_t>(m);
+    std::vector<double> hb(mm), hu(mm), hw(static_cast<size_t>(m));
+    SG_CUDA(cudaMemcpyAsync(hb.data(), B, sizeof(double) * mm, cudaMemcpyDeviceToHost, st));
+    SG_CUDA(cudaStreamSynchronize(st));
+    if (sg::symeig_host(m, hb.data(), hw.data(), hu.data()) != 0)
+      return sg::fail(SG_ERR_CUDA, "Rayleigh-Ritz: the host QL iteration did not converge (m=%d)", m);
+    SG_CUDA(cudaMemcpyAsync(B, hu.data(), sizeof(double) * mm, cudaMemcpyHostToDevice, st));
+    SG_CUDA(cudaMemcpyAsync(W, hw.data(), sizeof(double) * size_t(m), cudaMemcpyHostToDevice, st));
+    SG_CUDA(cudaStreamSynchronize(st));  // the host buffers go out of scope
+  }
+  (void)lwork_d;
   SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, Q, n, B, m, &zero, V, n));
   if (resid) {
     // A V = (A Q) U; the residual of Ritz pair c is (A Q) u_c - w_c v_c
@@ -596,6 +608,7 @@ extern "C" int sg_pca_basis_mixed(sg_handle* h, const double* cov, const double*
   double* W = cv.take<double>(n);
   double* tr = cv.take<double>(1);
   int* info = cv.take<int>(4);
+  SG_CUDA(cudaMemsetAsync(info, 0, 4 * sizeof(int), st));
   const int64_t ne = int64_t(nn);
   center_kernel<<<sg::ceil_div_i(ne, 256), 256, 0, st>>>(cov, zsum, 1.0 / double(n_used), n, A);
   SG_LAUNCH_CHECK();
@@ -735,22 +748,24 @@ struct FilterBufs {
   int cap_info;
 };
 
-// Y <- Y D L^-T with (Y D)^T (Y D) = L L^T and D the column scaling, twice
-// (FP32 Cholesky-QR2 on unit-norm columns). The first columns keep their
-// span: the block stays ordered with its dominant directions first.
-int cholqr2_f32(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, float* Y, int n, int m, FilterBufs& b,
-                cudaStream_t st) {
+// Y <- Y D L^-T with (Y D)^T (Y D) = L L^T and D the column scaling, in place
+// (FP32 Cholesky-QR on unit-norm columns), `passes` times. The first columns
+// keep their span: the block stays ordered with its dominant directions
+// first. One pass leaves the columns orthogonal to ~u cond(Y)^2, enough
+// between filter segments; two passes make them orthonormal to FP32.
+int cholqr_f32(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, float* Y, int n, int m, FilterBufs& b,
+               int passes, cudaStream_t st) {
   const float one = 1.f, zero = 0.f;
-  for (int pass = 0; pass < 2; ++pass) {
+  for (int pass = 0; pass < passes; ++pass) {
     SG_BLAS(cublasSgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Y, n, Y, n, &zero, b.G, m));
+    int* inf = b.info + std::min(b.n_info, b.cap_info - 3);
+    ++b.n_info;
     diag_copy_kernel<<<sg::ceil_div_i(m, 256), 256, 0, st>>>(b.G, b.D, m);
     SG_LAUNCH_CHECK();
     gram_scale_kernel<<<sg::ceil_div_i(int64_t(m) * m, 256), 256, 0, st>>>(b.G, b.D, m);
     SG_LAUNCH_CHECK();
     col_rscale_kernel<<<sg::ceil_div_i(int64_t(n) * m, 256), 256, 0, st>>>(Y, b.D, n, m);
     SG_LAUNCH_CHECK();
-    int* inf = b.info + std::min(b.n_info, b.cap_info - 1);
-    ++b.n_info;
     SG_SOLVER(cusolverDnSpotrf(sol, CUBLAS_FILL_MODE_LOWER, m, b.G, m, static_cast<float*>(h->solver_work),
                                int(h->solver_work_bytes / sizeof(float)), inf));
     SG_BLAS(cublasStrsm(blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, m, &one,
@@ -767,7 +782,7 @@ constexpr int kTailCols = 8;
 // *tail_rq receives the smallest Rayleigh quotient of the input block's last
 // kTailCols columns (host value; synchronises).
 int filter_segment(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, const float* A32, int n, int m, int deg,
-                   double cut, FilterBufs& b, cudaStream_t st, float* tail_rq) {
+                   double cut, FilterBufs& b, cudaStream_t st, float* tail_rq, int qr_passes) {
   const float a1 = float(2.0 / cut), a2 = float(4.0 / cut), m1 = -1.f, m2 = -2.f, one = 1.f;
   float* prev = b.X;
   float* cur = b.P;
@@ -784,7 +799,7 @@ int filter_segment(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, co
     SG_BLAS(cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &a2, A32, n, cur, n, &one, prev, n));
     std::swap(prev, cur);
   }
-  int rc = cholqr2_f32(h, sol, blas, cur, n, m, b, st);
+  int rc = cholqr_f32(h, sol, blas, cur, n, m, b, qr_passes, st);
   if (rc) return rc;
   SG_CUDA(cudaStreamSynchronize(st));
   float mn = INFINITY;
@@ -835,10 +850,12 @@ int cheb_degree(double t, double bound, int smax) {
 }  // namespace
 
 // Principal axes by Chebyshev-filtered block subspace iteration: FP32 cuBLAS
-// GEMMs apply Chebyshev polynomials of the centred scatter, damped on [0, cut]
-// (cut = the smallest Ritz value of the block, which never exceeds the
-// block's m-th eigenvalue, so no wanted pair is damped), to an m-wide block
-// that is re-orthonormalised (FP32 Cholesky-QR2) after each segment. An FP32
+// GEMMs apply Chebyshev polynomials of the centred scatter, damped on [0, cut],
+// to an m-wide block kept in descending order (dominant directions first),
+// re-orthogonalised by column-scaled FP32 Cholesky-QR after each segment. The
+// cut starts at the block's smallest Ritz value (never above its m-th
+// eigenvalue) and rises with the Rayleigh quotients of its last columns,
+// capped below the wanted pairs, so no wanted pair is damped. An FP32
 // Rayleigh-Ritz step picks the top n_comp + 16 Ritz vectors and the FP64
 // Rayleigh-Ritz step of the mixed solver refines them. If the FP64 residual
 // of a wanted pair exceeds 1e-4 of the largest eigenvalue, or the problem is
@@ -920,7 +937,7 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
                              std::max(sizeof(double) * size_t(lw_d), sizeof(double) * size_t(lw_dp)));
   rc = solver_work(h, wb);
   if (rc) return rc;
-  rc = cholqr2_f32(h, sol, blas, b.X, n, m, b, st);
+  rc = cholqr_f32(h, sol, blas, b.X, n, m, b, 2, st);
   if (rc) return rc;
   double hd[2];
   SG_CUDA(cudaMemcpyAsync(hd, tr, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -933,8 +950,8 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
   int deg = cheb_degree(2.0 * double(hrow) / cut - 1.0, 1e3, 8);
   EIG_DBG("filter: n=%d m=%d p=%d trace/n=%g rowmax=%g degA=%d\n", n, m, p, cut, double(hrow), deg);
   float rq = 0.f;
-  for (int s = 0; s < 2; ++s) {
-    rc = filter_segment(h, sol, blas, A32, n, m, deg, cut, b, st, &rq);
+  for (int s = 0; s < 2; ++s) {  // the second leaves X orthonormal for the Rayleigh-Ritz step
+    rc = filter_segment(h, sol, blas, A32, n, m, deg, cut, b, st, &rq, s == 1 ? 2 : 1);
     if (rc) return rc;
   }
   // phase B: cut from the block's smallest Ritz value, degree from its largest
@@ -968,7 +985,7 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
       const double t_max = 2.0 * theta_max / cut - 1.0;
       const bool last = done >= total;
       const int d = cheb_degree(t_max, last ? 1e2 : 1e5, 8);
-      rc = filter_segment(h, sol, blas, A32, n, m, d, cut, b, st, &rq);
+      rc = filter_segment(h, sol, blas, A32, n, m, d, cut, b, st, &rq, last && polish == 1 ? 2 : 1);
       if (rc) return rc;
       EIG_DBG("filter: seg %d deg %d cut %g tail_rq %g\n", segs, d, cut, double(rq));
       if (std::isfinite(rq)) cut = std::min(cut_cap, std::max(cut, double(rq)));
@@ -993,7 +1010,7 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
         ok = false;
       }
     EIG_DBG("filter: RR2 theta_min=%g theta_max=%g resid=%g\n", double(th[0]), double(th[size_t(m - 1)]), resid);
-    ok = ok && b.n_info < cap_info - 2 && resid <= 1e-4;
+    ok = ok && b.n_info < cap_info - 3 && resid <= 1e-4;
   }
   h->eig_resid = ok ? resid : INFINITY;
   if (!ok)
