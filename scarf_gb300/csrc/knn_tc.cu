@@ -35,14 +35,30 @@ constexpr int STAGES = 3;
 constexpr uint32_t A_BYTES = BM * BK * 2;
 constexpr uint32_t B_BYTES = BN * BK * 2;
 constexpr uint32_t TMEM_COLS = 512;
-constexpr int BUF = 64;  // candidate buffer slots per query row
+// 8 epilogue warps: two per TMEM lane quarter, each filtering one half of
+// every 256-column tile for its 32 rows with its own candidate list, so that
+// each scheduler has a second warp to issue while the other waits
+constexpr int EPI_WARPS = 8;
+constexpr int HALVES = EPI_WARPS / 4;
+constexpr int HCOLS = BN / HALVES;  // accumulator columns per epilogue warp
+constexpr int THREADS = 64 + 32 * EPI_WARPS;
+constexpr int BUF = 48;  // candidate buffer slots per (query row, half)
 __host__ __device__ constexpr size_t smem_bytes(int) {
-  return 1024 /*align*/ + A_BYTES + STAGES * B_BYTES + 256 /*barriers*/ + 4 * BN * 4 /*rn*/ +
-         size_t(BUF) * BM * 8 /*buffers*/;
+  return 1024 /*align*/ + A_BYTES + STAGES * B_BYTES + 256 /*barriers*/ + EPI_WARPS * BN * 4 /*rn*/ +
+         size_t(BUF) * BM * HALVES * 8 /*buffers*/ + size_t(HALVES) * BM * 4 /*published bounds*/;
 }
 
 // Instruction descriptor, kind::f16: D F32, A/B BF16, both K-major, N, M.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
+
+// Order-preserving map of a float to uint32 (for atomicMin across CTAs) and back.
+__device__ __forceinline__ uint32_t key_bits(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float bits_key(uint32_t u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
 
 template <int KC>
 struct TopK {
@@ -76,11 +92,14 @@ struct TopK {
   }
 };
 
-template <int KC>
-__global__ void __launch_bounds__(192, 1)
+// SHARE: the lists of a query share their worst keys (worth it when the
+// references are split over several CTAs; with one split the extra state
+// costs more than the candidates it saves)
+template <int KC, bool SHARE>
+__global__ void __launch_bounds__(THREADS, 1)
 knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const float* __restrict__ rn, int64_t nr, int64_t rps, int* __restrict__ cand, int64_t nq_pad,
-              int fold, int* __restrict__ err) {
+              int fold, unsigned* __restrict__ qbound, int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = su32(smem_raw);
   uint8_t* sm = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -94,8 +113,9 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   uint64_t* a_full = acc_empty + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(a_full + 1);
   float* rn_s = reinterpret_cast<float*>(sm + A_BYTES + STAGES * B_BYTES + 256);
-  float* bufk = rn_s + 4 * BN;                          // [BUF][BM]
-  int* bufi = reinterpret_cast<int*>(bufk + BUF * BM);  // [BUF][BM]
+  float* bufk = rn_s + EPI_WARPS * BN;                               // [BUF][HALVES * BM]
+  int* bufi = reinterpret_cast<int*>(bufk + BUF * BM * HALVES);      // [BUF][HALVES * BM]
+  float* pub = reinterpret_cast<float*>(bufi + BUF * BM * HALVES);   // [HALVES][BM] each list's worst
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t q0 = int64_t(blockIdx.x) * BM;
@@ -103,6 +123,7 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   const int64_t s_end = min(nr, s_begin + rps);
   const int ntiles = int((s_end - s_begin + BN - 1) / BN);
 
+  for (int i = threadIdx.x; i < HALVES * BM; i += blockDim.x) pub[i] = __int_as_float(0x7f800000);
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full[s], 1);
@@ -110,7 +131,7 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], 4);
+      mbar_init(&acc_empty[b], EPI_WARPS);
     }
     mbar_init(a_full, 1);
     fence_barrier_init();
@@ -181,22 +202,41 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
     }
   } else {
     const int quarter = warp & 3;  // TMEM lanes [32*quarter, 32*quarter+32) are this warp's
+    const int half = (warp - 2) / 4;  // accumulator columns [HCOLS*half, HCOLS*half + HCOLS)
     const int row = quarter * 32 + lane;
     float* my_rn = rn_s + (warp - 2) * BN;
-    float* bk = bufk + row;  // slot s of this row's candidate buffer: bk[s * BM]
-    int* bi = bufi + row;
+    float* bk = bufk + half * BM + row;  // slot s of this (row, half)'s buffer: bk[s * HALVES * BM]
+    int* bi = bufi + half * BM + row;
+    constexpr int SL = HALVES * BM;      // buffer slot stride
     TopK<KC> top;
     top.init();
-    float thr = __int_as_float(0x7f800000);
+    // Every list of a query (its two halves here, its reference splits in
+    // other CTAs) holds keys of that query, so each full list's worst key
+    // bounds the query's final KC-th key from above: a candidate at or above
+    // the smallest of them cannot make the query's top KC. The halves share
+    // their worst keys through shared memory, the splits through `qbound`
+    // (atomicMin on an order-preserving encoding); both only decrease, so a
+    // stale value is still a valid bound.
+    unsigned* qb = qbound + q0 + row;
+    float* my_pub = pub + half * BM + row;
+    const float* other_pub = pub + (half ^ 1) * BM + row;
+    float shared = __int_as_float(0x7f800000);  // smallest worst key of the other lists
+    float thr = shared;
     int cnt = 0;
-    // merge the buffered candidates into the sorted register list
+    // merge the buffered candidates into the sorted register list, then
+    // publish the list's worst key
     auto compact = [&]() {
       for (int s2 = 0; s2 < cnt; ++s2) {
-        const float v = bk[s2 * BM];
-        if (v < top.worst()) top.insert(v, bi[s2 * BM]);
+        const float v = bk[s2 * SL];
+        if (v < top.worst() && (!SHARE || v < shared)) top.insert(v, bi[s2 * SL]);
       }
       cnt = 0;
-      thr = top.worst();
+      const float w = top.worst();
+      if (SHARE && w < *my_pub) {
+        *my_pub = w;
+        atomicMin(qb, key_bits(w));
+      }
+      thr = SHARE ? fminf(w, shared) : w;
     };
     // filter one chunk of 32 accumulator columns into the buffer; kRn: add
     // |r|^2 here (not folded into the MMA); kMask: last tile, columns >= lim
@@ -221,8 +261,8 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
             if (kk[q] < thr) {
-              bk[cnt * BM] = kk[q];
-              bi[cnt * BM] = cbase + j + q;
+              bk[cnt * SL] = kk[q];
+              bi[cnt * SL] = cbase + j + q;
               ++cnt;
             }
           }
@@ -250,25 +290,31 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
         reinterpret_cast<float4*>(my_rn)[lane * 2] = __ldg(src + lane * 2);
         reinterpret_cast<float4*>(my_rn)[lane * 2 + 1] = __ldg(src + lane * 2 + 1);
       }
+      if (SHARE) {
+        shared = fminf(shared, fminf(*other_pub, bits_key(__ldcg(qb))));
+        thr = fminf(thr, shared);
+      }
       bool ok = mbar_wait(&acc_full[b], aph, err, 5);
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) break;
       tc_fence_after();
       __syncwarp();
-      const uint32_t tbase = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(b * BN);
+      const uint32_t tbase = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(b * BN + half * HCOLS);
+      constexpr int NCH = HCOLS / 32;
+      const int ch0 = half * NCH;  // this warp's first 32-column chunk of the tile
       uint32_t ra[32], rb[32];
       tmem_ld32(tbase, ra);
       tmem_wait_ld(ra);
 #pragma unroll 1
-      for (int ch = 0; ch < BN / 32; ch += 2) {
+      for (int ch = 0; ch < NCH; ch += 2) {
         tmem_ld32(tbase + uint32_t((ch + 1) * 32), rb);
         if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
-        filter(ra, ch, r0, lim);
+        filter(ra, ch0 + ch, r0, lim);
         tmem_wait_ld(rb);
-        if (ch + 2 < BN / 32) tmem_ld32(tbase + uint32_t((ch + 2) * 32), ra);
+        if (ch + 2 < NCH) tmem_ld32(tbase + uint32_t((ch + 2) * 32), ra);
         if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
-        filter(rb, ch + 1, r0, lim);
-        if (ch + 2 < BN / 32) tmem_wait_ld(ra);
+        filter(rb, ch0 + ch + 1, r0, lim);
+        if (ch + 2 < NCH) tmem_wait_ld(ra);
       }
       tc_fence_before();
       __syncwarp();
@@ -276,7 +322,8 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       __syncwarp();
     }
     compact();
-    int* out = cand + (int64_t(blockIdx.y) * nq_pad + q0 + row) * KC;
+    // list (split, half) of every query: nsplit * HALVES lists per query
+    int* out = cand + ((int64_t(blockIdx.y) * HALVES + half) * nq_pad + q0 + row) * KC;
 #pragma unroll
     for (int j = 0; j < KC; ++j) out[j] = top.i[j];
   }
@@ -332,11 +379,16 @@ __global__ void queries_bf16_kernel(const float* __restrict__ in, int64_t n, int
 
 template <int KC>
 int launch_tc(const CUtensorMap& a, const CUtensorMap& b, const float* rn, int64_t nr, int64_t rps, int nsplit,
-              int* cand, int64_t nq_pad, int fold, int* err, cudaStream_t st) {
+              int* cand, int64_t nq_pad, int fold, unsigned* qbound, int* err, cudaStream_t st) {
   const size_t smem = smem_bytes(KC);
-  SG_CUDA(cudaFuncSetAttribute(knn_tc_kernel<KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   dim3 grid(unsigned(nq_pad / BM), unsigned(nsplit));
-  knn_tc_kernel<KC><<<grid, 192, smem, st>>>(a, b, rn, nr, rps, cand, nq_pad, fold, err);
+  if (nsplit > 1) {
+    SG_CUDA(cudaFuncSetAttribute(knn_tc_kernel<KC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    knn_tc_kernel<KC, true><<<grid, THREADS, smem, st>>>(a, b, rn, nr, rps, cand, nq_pad, fold, qbound, err);
+  } else {
+    SG_CUDA(cudaFuncSetAttribute(knn_tc_kernel<KC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    knn_tc_kernel<KC, false><<<grid, THREADS, smem, st>>>(a, b, rn, nr, rps, cand, nq_pad, fold, qbound, err);
+  }
   SG_LAUNCH_CHECK();
   return SG_OK;
 }
@@ -363,7 +415,8 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   const int fold = d <= BK - 3 ? 1 : 0;
   const size_t need = sg::Carver::need(size_t(nr_pad) * BK * 2) + sg::Carver::need(size_t(nr_pad) * 4) +
                       sg::Carver::need(size_t(nq_pad) * BK * 2) +
-                      sg::Carver::need(sizeof(int) * size_t(nsplit) * nq_pad * kc) + sg::Carver::need(sizeof(int));
+                      sg::Carver::need(sizeof(int) * size_t(nsplit) * HALVES * nq_pad * kc) + sg::Carver::need(sizeof(int)) +
+                      sg::Carver::need(sizeof(unsigned) * size_t(nq_pad));
   int status;
   void* w = sg::ws_get(h, need, &status);
   if (!w) return status;
@@ -371,9 +424,12 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   __nv_bfloat16* Rb = cv.take<__nv_bfloat16>(size_t(nr_pad) * BK);
   float* rn = cv.take<float>(nr_pad);
   __nv_bfloat16* Qb = cv.take<__nv_bfloat16>(size_t(nq_pad) * BK);
-  int* cand = cv.take<int>(size_t(nsplit) * nq_pad * kc);
+  int* cand = cv.take<int>(size_t(nsplit) * HALVES * nq_pad * kc);
   int* err = cv.take<int>(1);
+  unsigned* qbound = cv.take<unsigned>(size_t(nq_pad));
   SG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+  // all ones: decodes to NaN, which fminf ignores (no bound yet)
+  SG_CUDA(cudaMemsetAsync(qbound, 0xFF, sizeof(unsigned) * size_t(nq_pad), st));
   refs_bf16_kernel<<<sg::ceil_div_i(nr_pad, 256), 256, 0, st>>>(refs, nr, d, ld, fold, Rb, nr_pad, rn);
   SG_LAUNCH_CHECK();
   queries_bf16_kernel<<<sg::ceil_div_i(nq_pad, 256), 256, 0, st>>>(queries, nq, d, ld, fold, Qb, nq_pad);
@@ -385,11 +441,11 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   if (rc) return rc;
   {
   sg::ProfScope prof(h, "knn_tc", st);
-  if (kc == 16) rc = launch_tc<16>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, err, st);
-  else if (kc == 32) rc = launch_tc<32>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, err, st);
-  else if (kc == 40) rc = launch_tc<40>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, err, st);
-  else if (kc == 48) rc = launch_tc<48>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, err, st);
-  else rc = launch_tc<64>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, err, st);
+  if (kc == 16) rc = launch_tc<16>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, st);
+  else if (kc == 32) rc = launch_tc<32>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, st);
+  else if (kc == 40) rc = launch_tc<40>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, st);
+  else if (kc == 48) rc = launch_tc<48>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, st);
+  else rc = launch_tc<64>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, st);
   }
   if (rc) return rc;
   int herr = 0;
@@ -397,6 +453,6 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   SG_CUDA(cudaStreamSynchronize(st));
   if (herr) return sg::fail(SG_ERR_TIMEOUT, "sg_knn: a tensor-core pipeline wait expired (stage %d)", herr);
   sg::ProfScope prof(h, "rerank", st);
-  return sg_rerank(queries, refs, d, ld, nq, cand, nsplit, kc, nq_pad, kq, k, self_offset, idx_out, dist_out, nmiss,
-                   st);
+  return sg_rerank(queries, refs, d, ld, nq, cand, nsplit * HALVES, kc, nq_pad, kq, k, self_offset, idx_out, dist_out,
+                   nmiss, st);
 }
