@@ -776,6 +776,15 @@ int cholqr_f32(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, float*
 
 constexpr int kTailCols = 8;
 
+// C = alpha A B + beta C for the filter's n x n by n x m products: FP32 inputs
+// and outputs, computed by cuBLAS as FP32 emulated with BF16 splits on the
+// tensor cores (the accuracy of an FP32 GEMM, about 20% faster here)
+cublasStatus_t filter_gemm(cublasHandle_t blas, int n, int m, const float* alpha, const float* A, const float* B,
+                           const float* beta, float* C) {
+  return cublasGemmEx(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, alpha, A, CUDA_R_32F, n, B, CUDA_R_32F, n, beta, C,
+                      CUDA_R_32F, n, CUBLAS_COMPUTE_32F_EMULATED_16BFX9, CUBLAS_GEMM_DEFAULT);
+}
+
 // One filter segment on the block X: X <- orth(T_deg((2A - cut I)/cut) X),
 // the Chebyshev polynomial that is bounded by 1 on [0, cut] and grows fastest
 // above it. Recurrence: Y1 = (2/cut) A X - X, Y_{k+1} = (4/cut) A Y_k - 2 Y_k - Y_{k-1}.
@@ -787,7 +796,7 @@ int filter_segment(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, co
   float* prev = b.X;
   float* cur = b.P;
   SG_CUDA(cudaMemcpyAsync(cur, prev, sizeof(float) * size_t(n) * m, cudaMemcpyDeviceToDevice, st));
-  SG_BLAS(cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &a1, A32, n, prev, n, &m1, cur, n));
+  SG_BLAS(filter_gemm(blas, n, m, &a1, A32, prev, &m1, cur));
   const int K = std::min(kTailCols, m);
   tail_rq_kernel<<<K, 256, 0, st>>>(prev, cur, n, m, K, a1, b.R);
   SG_LAUNCH_CHECK();
@@ -796,7 +805,7 @@ int filter_segment(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, co
   for (int k = 2; k <= deg; ++k) {
     // prev <- -prev - 2 cur, then prev <- (4/cut) A cur + prev
     SG_BLAS(cublasSgeam(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, &m1, prev, n, &m2, cur, n, prev, n));
-    SG_BLAS(cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &a2, A32, n, cur, n, &one, prev, n));
+    SG_BLAS(filter_gemm(blas, n, m, &a2, A32, cur, &one, prev));
     std::swap(prev, cur);
   }
   int rc = cholqr_f32(h, sol, blas, cur, n, m, b, qr_passes, st);
@@ -819,7 +828,7 @@ int filter_segment(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, co
 int ritz_f32(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, const float* A32, int n, int m, FilterBufs& b,
              int lwork_s, std::vector<float>& wh, bool vectors, cudaStream_t st) {
   const float one = 1.f, zero = 0.f;
-  SG_BLAS(cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &one, A32, n, b.X, n, &zero, b.P, n));
+  SG_BLAS(filter_gemm(blas, n, m, &one, A32, b.X, &zero, b.P));
   SG_BLAS(cublasSgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, b.X, n, b.P, n, &zero, b.G, m));
   int* inf = b.info + std::min(b.n_info, b.cap_info - 1);
   ++b.n_info;
@@ -968,30 +977,56 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
     // value of pair n_comp + 8, which is a lower bound of that eigenvalue: no
     // wanted pair is ever damped.
     cut = double(th[0]);
-    const double theta_w = double(th[size_t(m - std::min(m, n_comp + 8))]);
-    const double cut_cap = 0.99 * theta_w;
-    const double theta_max = 1.05 * double(th[size_t(m - 1)]);
-    const double t_w = 2.0 * theta_w / cut - 1.0;
-    const double rate = t_w > 1.0 ? std::acosh(t_w) : 0.0;
-    int total = rate > 0.0 ? int(std::ceil(std::log(1e10) / rate)) : 240;
-    total = std::min(240, std::max(total, 8));
+    double theta_w = double(th[size_t(m - std::min(m, n_comp + 8))]);
+    double cut_cap = 0.99 * theta_w;
+    double theta_max = 1.05 * double(th[size_t(m - 1)]);
+    // Degree budget: each segment amplifies pair n_comp over the damped
+    // interval by about exp(deg * acosh(t)), t = 2 theta_c / cut - 1 for the
+    // cut it ran with; stop when the product reaches 1e10. A flat spectrum
+    // near the cut (many cells: a narrow Marchenko-Pastur bulk) gets more
+    // segments, a well separated one fewer.
+    double theta_c = double(th[size_t(m - std::min(m, n_comp))]);
+    const double target = std::log(1e10);
+    double gain = 0.0;
+    int done = 0, segs = 0;
+    bool refreshed = false;
+    EIG_DBG("filter: RR1 theta_min=%g theta_c=%g theta_w=%g theta_max=%g\n", double(th[0]), theta_c, theta_w,
+            double(th[size_t(m - 1)]));
     // long segments while the dominant directions lead the block (their
     // growth over the weakest column at most 1e5), then two short ones
     // (growth at most 1e2) that leave the block accurate to FP32
-    int done = 0, segs = 0;
-    EIG_DBG("filter: RR1 theta_min=%g theta_w=%g theta_max=%g t_w=%g total=%d\n", double(th[0]), theta_w,
-            double(th[size_t(m - 1)]), t_w, total);
-    for (int polish = 0; done < total || polish < 2; ++segs) {
+    for (int polish = 0; gain < target || polish < 2; ++segs) {
       const double t_max = 2.0 * theta_max / cut - 1.0;
-      const bool last = done >= total;
+      const bool last = gain >= target;
       const int d = cheb_degree(t_max, last ? 1e2 : 1e5, 8);
       rc = filter_segment(h, sol, blas, A32, n, m, d, cut, b, st, &rq, last && polish == 1 ? 2 : 1);
       if (rc) return rc;
-      EIG_DBG("filter: seg %d deg %d cut %g tail_rq %g\n", segs, d, cut, double(rq));
+      if (!last) {
+        gain += d * std::acosh(std::max(1.0, 2.0 * theta_c / cut - 1.0));
+        done += d;
+      }
+      EIG_DBG("filter: seg %d deg %d cut %g tail_rq %g gain %g\n", segs, d, cut, double(rq), gain);
+      if (!last && !refreshed && std::isfinite(rq) && double(rq) > cut_cap && gain > 0.25 * target) {
+        // The cap, from Ritz values of a barely filtered block, holds the cut
+        // below the block's tail: fresh Ritz values (of the orthonormalised
+        // block, which they also put in descending order) give a higher,
+        // still valid cap and a better rate estimate.
+        rc = cholqr_f32(h, sol, blas, b.X, n, m, b, 1, st);
+        if (rc) return rc;
+        rc = ritz_f32(h, sol, blas, A32, n, m, b, lw_s, th, true, st);
+        if (rc) return rc;
+        refreshed = true;
+        if (th[0] > 0.f && std::isfinite(th[size_t(m - 1)])) {
+          theta_w = std::max(theta_w, double(th[size_t(m - std::min(m, n_comp + 8))]));
+          theta_c = std::max(theta_c, double(th[size_t(m - std::min(m, n_comp))]));
+          theta_max = std::max(theta_max, 1.05 * double(th[size_t(m - 1)]));
+          cut_cap = 0.99 * theta_w;
+        }
+        EIG_DBG("filter: refresh theta_c=%g theta_w=%g\n", theta_c, theta_w);
+      }
       if (std::isfinite(rq)) cut = std::min(cut_cap, std::max(cut, double(rq)));
       if (last) ++polish;
-      else done += d;
-      if (segs > 120) break;
+      if (done >= 240 && !last) gain = target;  // degree cap
     }
     rc = ritz_f32(h, sol, blas, A32, n, m, b, lw_s, th, true, st);
     if (rc) return rc;

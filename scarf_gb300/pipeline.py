@@ -77,7 +77,8 @@ def normalize_csr_host(indptr, indices, data, n_genes: int, feat_idx, *, size_fa
                        device="cuda", missing_mask=None, fill_value=1.0, cmap=None):
     """a1+a3 over host (ideally pinned) CSR arrays. With ``chunk_cells`` the rows
     are streamed: chunk i+1 is copied on a side stream while chunk i is
-    normalised. Returns ``(x, colsum, colsumsq)``."""
+    normalised. Host inputs are streamed in about 8 chunks unless
+    ``chunk_cells`` says otherwise (0: one copy). Returns ``(x, colsum, colsumsq)``."""
     dev = torch.device(device)
     h = len(feat_idx)
     n = len(indptr) - 1
@@ -95,6 +96,8 @@ def normalize_csr_host(indptr, indices, data, n_genes: int, feat_idx, *, size_fa
         ind_h = ind_h.to(torch.int32)
     if dat_h.dtype != torch.int32:
         dat_h = dat_h.to(torch.int32)
+    if chunk_cells is None and ind_h.device.type == "cpu":
+        chunk_cells = max(16384, -(-n // 8))
     if not chunk_cells or chunk_cells >= n:
         ip = ip_h.to(dev, non_blocking=True)
         ind = ind_h.to(dev, non_blocking=True)
