@@ -54,6 +54,8 @@ SEED = 4466
 # cuSOLVER call; every other name is a kernel of this repository)
 PROFILED = ("normalize", "zsplit", "cov_tc", "cov_simt", "eigh", "project", "knn_tc", "knn_simt", "rerank",
             "smooth", "union")
+# parts of the filtered eigensolver (inside "eigh")
+EIG_PARTS = ("eig_filter", "eig_qr", "eig_rr32", "eig_rr64")
 
 
 def dist_env():
@@ -365,6 +367,10 @@ def run_gb300(args, cfg):
                 t, c = K.profile_query(name)
                 if c:
                     prof_ms[name] = (t / c, c / steps)
+            for name in EIG_PARTS:
+                t, c = K.profile_query(name)
+                if c:
+                    eig_parts[name] = {"ms_per_step": round(t / steps, 3), "calls_per_step": c / steps}
             K.profile(False)
         if ws > 1:
             t = torch.tensor([ms], device=dev, dtype=torch.float64)
@@ -372,13 +378,14 @@ def run_gb300(args, cfg):
             ms = float(t.item())
         return ms, res, launches, prof_ms, outs
 
+    eig_parts = {}
     sampler = ClockSampler(local)
     sampler.start()
     ms, res, launches, prof_ms, _ = timed("precision", args.steps, args.warmup, prof=True)
     clocks = sampler.stop()
     rec, werr = graph_check(res, BATCH)
     ann_recall = res.recall()
-    e2e_ms, res_h, _, _, outs = timed("precision", args.steps, max(1, min(args.warmup, 2)), host=True)
+    e2e_ms, res_h, _, _, outs = timed("precision", args.steps, args.warmup, host=True)
     plain_ms, res_p, _, prof_p, _ = timed("plain", max(1, min(args.steps, 3)), 1, prof=True)
     rec_p, werr_p = graph_check(res_p, BATCH)
     truth = fp64_truth(K, pipeline, ip_d, ind_d, dat_d, G, feat, dims, k, {"precision": res, "plain": res_p})
@@ -453,6 +460,7 @@ def run_gb300(args, cfg):
                   "vs_fp64_pipeline": truth["plain"], "speedup_precision_vs_plain": round(plain_ms / ms, 3),
                   "kernels_ms": {k_: round(v[0], 4) for k_, v in prof_p.items()}},
         "kernels": kernels,
+        "eigh_parts": eig_parts,
         "eigensolver": eig,
         "e2e": {"value": round(cells / (e2e_ms * 1e-3), 1), "unit": "cells/s", "ms_per_step": round(e2e_ms, 3),
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -600,10 +608,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--mode", default="full", choices=["full", "step", "serve"],
+    ap.add_argument("--mode", default="full", choices=["full", "step", "serve", "knn"],
                     help="step: warm-up steps then one make_graph step and nothing else (for profilers); "
                          "serve: the mapping service's latency under a Poisson request stream")
     ap.add_argument("--form", default="precision", choices=["precision", "plain"], help="form used by --mode step")
+    ap.add_argument("--knn-queries", type=int, default=110_000, help="--mode knn: query rows")
+    ap.add_argument("--knn-refs", type=int, default=1_000_000, help="--mode knn: reference rows")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "gb300" else args.warmup
     cfg = CONFIGS[args.config]
@@ -613,6 +623,8 @@ def main():
         run_step(args, cfg)
     elif args.mode == "serve":
         run_serve(args)
+    elif args.mode == "knn":
+        run_knn(args)
     else:
         run_gb300(args, cfg)
 
@@ -671,7 +683,7 @@ def run_serve(args):
         t_end = max(r.t_done for r in reqs)
         batches = srv.batches_run
         blog = np.array(srv.batch_log[3:], dtype=np.float64).reshape(-1, 2)
-        ulog = np.array(srv.upload_log[3:], dtype=np.float64).reshape(-1, 2)
+        ulog = np.array(srv.upload_log[3:], dtype=np.float64).reshape(-1, 5)
     summ = latency_summary(reqs)
     small = latency_summary([r for r in reqs if r.n_cells <= 10_000])
     # recall of one mid-size request against exact FP64 kNN on the device
@@ -701,11 +713,46 @@ def run_serve(args):
         "batch_rows_mean": round(float(blog[:, 0].mean()), 1) if len(blog) else None,
         "batch_ms_p50": round(float(np.percentile(blog[:, 1], 50)) * 1e3, 3) if len(blog) else None,
         "batch_ms_p99": round(float(np.percentile(blog[:, 1], 99)) * 1e3, 3) if len(blog) else None,
-        "upload_ms_p50": round(float(np.percentile(ulog[:, 1], 50)) * 1e3, 3) if len(ulog) else None,
-        "upload_ms_p99": round(float(np.percentile(ulog[:, 1], 99)) * 1e3, 3) if len(ulog) else None,
+        "upload_ms_p50": round(float(np.percentile(ulog[:, 3:].sum(1), 50)) * 1e3, 3) if len(ulog) else None,
+        "upload_ms_p99": round(float(np.percentile(ulog[:, 3:].sum(1), 99)) * 1e3, 3) if len(ulog) else None,
+        "upload_queue_ms_p99": round(float(np.percentile(ulog[:, 2], 99)) * 1e3, 3) if len(ulog) else None,
+        "slowest_uploads": [{"cells": int(u[0]), "MB": round(u[1] / 1e6, 1), "queued_ms": round(u[2] * 1e3, 2),
+                             "issue_ms": round(u[3] * 1e3, 2), "land_ms": round(u[4] * 1e3, 2)}
+                            for u in sorted(ulog.tolist(), key=lambda u: -(u[3] + u[4]))[:4]],
         "recall_at_k_sampled_request": round(rec, 5), "data": "synthetic",
         "config": {"workload": c["name"], "arrival_rate_hz": c["rate_hz"], "max_batch_rows": c["max_batch_rows"],
                    "workers": 2, "form": "precision"}}), flush=True)
+
+
+def run_knn(args):
+    """The kNN kernel alone (profiling case): seeded clustered points (40
+    centres, N(0, 1) offsets, d = 50), the first --knn-queries rows against
+    all --knn-refs rows, k = 21, margin 16, the precision form; W warm-up
+    calls and one more."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from scarf_gb300 import kernels as K
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    n, d, ld = args.knn_refs, 50, 52
+    centers = torch.randn((40, d), generator=g, device=dev) * 4.0
+    lab = torch.randint(0, 40, (n,), generator=g, device=dev)
+    refs = torch.zeros((n, ld), device=dev)
+    refs[:, :d] = centers[lab] + torch.randn((n, d), generator=g, device=dev)
+    q = refs[:args.knn_queries].contiguous()
+    self_offset = 0 if args.knn_queries <= n else -1
+    for _ in range(args.warmup):
+        K.knn(q, refs, d, 21, self_offset=self_offset, margin=16, precision="precision")
+    K.profile(True)
+    K.profile_reset()
+    idx, dist, nm = K.knn(q, refs, d, 21, self_offset=self_offset, margin=16, precision="precision")
+    torch.cuda.synchronize()
+    t, _ = K.profile_query("knn_tc")
+    t2, _ = K.profile_query("rerank")
+    K.profile(False)
+    print(json.dumps({"mode": "knn", "queries": int(q.shape[0]), "refs": n, "knn_tc_ms": round(t, 3),
+                      "rerank_ms": round(t2, 3), "missed": int(nm.item())}))
 
 
 def run_step(args, cfg):

@@ -159,6 +159,122 @@ __global__ void normalize_kernel(const int64_t* __restrict__ indptr,
   }
 }
 
+// FP32 output without fused statistics: the same per-row arithmetic as
+// normalize_kernel, but every warp walks its own rows (grid-stride) with no
+// CTA-wide barrier, so a long row never holds the other warps of its CTA.
+// The column statistics then come from colstats_kernel over the output.
+template <typename CM>
+__global__ void __launch_bounds__(256)
+normalize_rows_kernel(const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                      const int32_t* __restrict__ data, int64_t n_rows, const CM* __restrict__ col_map,
+                      int64_t n_genes, int n_cols, int vec, int pitch, const uint8_t* __restrict__ missing, float fill,
+                      const double* __restrict__ n_counts, float sf, unsigned flags, float* __restrict__ out,
+                      int64_t ld_out, int64_t* __restrict__ libsize_out) {
+  extern __shared__ __align__(16) float smem[];
+  const int nwarps = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* row = smem + warp * pitch;
+  float4* row4 = reinterpret_cast<float4*>(row);
+  const bool renorm = flags & SG_NORM_RENORM_SUBSET;
+  const bool do_log = flags & SG_NORM_LOG1P;
+  const int64_t base = indptr[0];
+  const int64_t stride = int64_t(gridDim.x) * nwarps;
+  for (int64_t r = int64_t(blockIdx.x) * nwarps + warp; r < n_rows; r += stride) {
+    for (int j = lane; j < pitch / 4; j += 32) row4[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
+    long long s = 0;
+    const int64_t p0 = indptr[r] - base, p1 = indptr[r + 1] - base;
+    auto take = [&](int g, int c) {
+      const int m = (unsigned)g < (unsigned long long)n_genes ? int(col_map[g]) : -1;
+      if ((unsigned)m < (unsigned)n_cols) {
+        s += c;
+        atomicAdd(&row[m], float(c));
+      }
+    };
+    if (vec) {
+      const int mis = int((reinterpret_cast<uintptr_t>(indices + p0) & 15) >> 2);
+      const int64_t pa = min(p1, p0 + ((4 - mis) & 3));
+      if (p0 + lane < pa) take(indices[p0 + lane], data[p0 + lane]);
+      int64_t q = pa + 4 * lane;
+      // four 16-byte pairs in flight per lane
+      for (; q + 387 < p1; q += 512) {
+        int4 g[4], c[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          g[u] = __ldcs(reinterpret_cast<const int4*>(indices + q + 128 * u));
+          c[u] = __ldcs(reinterpret_cast<const int4*>(data + q + 128 * u));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          take(g[u].x, c[u].x); take(g[u].y, c[u].y); take(g[u].z, c[u].z); take(g[u].w, c[u].w);
+        }
+      }
+      for (; q + 3 < p1; q += 128) {
+        const int4 g0 = __ldcs(reinterpret_cast<const int4*>(indices + q));
+        const int4 c0 = __ldcs(reinterpret_cast<const int4*>(data + q));
+        take(g0.x, c0.x); take(g0.y, c0.y); take(g0.z, c0.z); take(g0.w, c0.w);
+      }
+      for (int64_t e = q; e < p1 && e < q + 4; ++e) take(indices[e], data[e]);
+    } else {
+      int64_t p = p0 + lane;
+      for (; p + 96 < p1; p += 128) {
+        const int g0 = indices[p], g1 = indices[p + 32], g2 = indices[p + 64], g3 = indices[p + 96];
+        const int c0 = data[p], c1 = data[p + 32], c2 = data[p + 64], c3 = data[p + 96];
+        take(g0, c0); take(g1, c1); take(g2, c2); take(g3, c3);
+      }
+      for (; p < p1; p += 32) take(indices[p], data[p]);
+    }
+    s = warp_sum_ll(s);
+    const double scal = renorm ? ((s == 0) ? 1.0 : double(s)) : n_counts[r];
+    const float sc = float(scal);
+    __syncwarp();
+    float4* o4 = reinterpret_cast<float4*>(out + r * ld_out);
+    for (int j4 = lane; j4 < pitch / 4; j4 += 32) {
+      float4 c4 = row4[j4];
+      float* cv = reinterpret_cast<float*>(&c4);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int j = 4 * j4 + u;
+        float v;
+        if (cv[u] == 0.f && sc != 0.f) {
+          v = 0.f;
+        } else {
+          v = __fdiv_rn(sf * cv[u], sc);
+          if (do_log) v = log1pf(v);
+        }
+        if (missing && j < n_cols && missing[j]) v = fill;
+        cv[u] = j < n_cols ? v : 0.f;
+      }
+      if (4 * j4 + 3 < n_cols) {
+        __stcs(o4 + j4, c4);
+      } else {
+        for (int u = 0; u < 4 && 4 * j4 + u < n_cols; ++u) out[r * ld_out + 4 * j4 + u] = cv[u];
+      }
+    }
+    if (libsize_out && renorm && lane == 0) libsize_out[r] = (s == 0) ? 1 : s;
+    __syncwarp();
+  }
+}
+
+// Per-CTA column sums of x and x^2 over rows [blockIdx.x * rows, +rows), one
+// thread per column slice, rows in order (reproducible run to run).
+__global__ void __launch_bounds__(256)
+colstats_kernel(const float* __restrict__ x, int64_t n_rows, int n_cols, int64_t ld, int rows,
+                float* __restrict__ part_sum, float* __restrict__ part_sq) {
+  const int64_t r0 = int64_t(blockIdx.x) * rows;
+  const int64_t r1 = min(n_rows, r0 + rows);
+  for (int j = threadIdx.x; j < n_cols; j += blockDim.x) {
+    float a = 0.f, b = 0.f;
+    for (int64_t r = r0; r < r1; ++r) {
+      const float v = __ldcs(x + r * ld + j);
+      a += v;
+      b = fmaf(v, v, b);
+    }
+    part_sum[int64_t(blockIdx.x) * n_cols + j] = a;
+    part_sq[int64_t(blockIdx.x) * n_cols + j] = b;
+  }
+}
+
 // Stage 1 of the FP64 reduction: group g sums partial rows [g*per, (g+1)*per).
 __global__ void partial_reduce1(const float* __restrict__ ps, const float* __restrict__ pq, int nparts,
                                 int n_cols, int per, double* __restrict__ gs, double* __restrict__ gq) {
@@ -245,13 +361,18 @@ extern "C" int sg_normalize_csr(sg_handle* h, const int64_t* indptr, const int32
 
   const int pitch = (n_cols + 3) & ~3;
   const size_t row_bytes = size_t(pitch) * sizeof(float);
+  const bool f32 = out_dtype == SG_F32;
+  // FP32 output: barrier-free rows, then column statistics over the output
+  // (kStatRows rows per CTA); BF16 output: the fused kernel, whose statistics
+  // come from the unrounded values
+  constexpr int kStatRows = 256;
   int nwarps = 8;
-  while (nwarps > 1 && (size_t(nwarps) + 2) * row_bytes > h->smem_optin) --nwarps;
-  const size_t smem = (size_t(nwarps) + 2) * row_bytes;
+  while (nwarps > 1 && (size_t(nwarps) + (f32 ? 0 : 2)) * row_bytes > h->smem_optin) --nwarps;
+  const size_t smem = (size_t(nwarps) + (f32 ? 0 : 2)) * row_bytes;
   if (smem > h->smem_optin)
     return sg::fail(SG_ERR_UNSUPPORTED, "sg_normalize_csr: %d output columns exceed the shared-memory row buffer", n_cols);
   const int64_t rows_per_cta = int64_t(nwarps) * kRounds;
-  const int nblocks = sg::ceil_div_i(n_rows, rows_per_cta);
+  const int nblocks = f32 ? sg::ceil_div_i(n_rows, kStatRows) : sg::ceil_div_i(n_rows, rows_per_cta);
 
   const bool narrow = n_cols < 32768;
   float* ps = nullptr;
@@ -287,6 +408,17 @@ extern "C" int sg_normalize_csr(sg_handle* h, const int64_t* indptr, const int32
   const int vec = ((reinterpret_cast<uintptr_t>(indices) ^ reinterpret_cast<uintptr_t>(data)) & 15) == 0 ? 1 : 0;
   const float sf = float(size_factor);
   sg::ProfScope prof(h, "normalize", st);
+  auto launch_rows = [&](auto kern, const auto* map) -> int {
+    SG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    int per_sm = 0;
+    SG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nwarps * 32, smem));
+    const int64_t grid = std::min<int64_t>(sg::ceil_div(n_rows, nwarps), int64_t(std::max(1, per_sm)) * h->sm_count);
+    kern<<<unsigned(grid), nwarps * 32, smem, st>>>(indptr, indices, data, n_rows, map, n_genes, n_cols, vec, pitch,
+                                                    missing_mask, fill_value, n_counts, sf, flags,
+                                                    static_cast<float*>(out), ld_out, libsize_out);
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+  };
   auto launch = [&](auto kern, const auto* map) -> int {
     SG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     kern<<<nblocks, nwarps * 32, smem, st>>>(indptr, indices, data, n_rows, map, n_genes, n_cols, vec, pitch,
@@ -296,10 +428,17 @@ extern "C" int sg_normalize_csr(sg_handle* h, const int64_t* indptr, const int32
     return SG_OK;
   };
   int rc;
-  if (out_dtype == SG_F32)
-    rc = narrow ? launch(normalize_kernel<false, int16_t>, map16) : launch(normalize_kernel<false, int32_t>, col_map);
-  else
+  if (f32) {
+    rc = narrow ? launch_rows(normalize_rows_kernel<int16_t>, map16) : launch_rows(normalize_rows_kernel<int32_t>, col_map);
+    if (rc) return rc;
+    if (colsum) {
+      colstats_kernel<<<nblocks, 256, 0, st>>>(static_cast<const float*>(out), n_rows, n_cols, ld_out, kStatRows, ps,
+                                               pq);
+      SG_LAUNCH_CHECK();
+    }
+  } else {
     rc = narrow ? launch(normalize_kernel<true, int16_t>, map16) : launch(normalize_kernel<true, int32_t>, col_map);
+  }
   if (rc) return rc;
   if (colsum) {
     dim3 g1(sg::ceil_div_i(n_cols, 256), ngroups);

@@ -503,6 +503,7 @@ int rayleigh_ritz_fp64(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas
                        double* Q, double* Y, double* V, double* G, double* B, double* W, int* info, int lwork_d,
                        int n_top, double* resid, double* rcol, cudaStream_t st) {
   const double one = 1.0, zero = 0.0;
+  sg::ProfScope prof(h, "eig_rr64", st);
   // Q <- Q R^-1 with Q^T Q = L L^T (R = L^T): FP64 Cholesky-QR
   SG_BLAS(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Q, n, Q, n, &zero, G, m));
   SG_SOLVER(cusolverDnDpotrf(sol, CUBLAS_FILL_MODE_LOWER, m, G, m, static_cast<double*>(h->solver_work),
@@ -756,6 +757,7 @@ struct FilterBufs {
 int cholqr_f32(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, float* Y, int n, int m, FilterBufs& b,
                int passes, cudaStream_t st) {
   const float one = 1.f, zero = 0.f;
+  sg::ProfScope prof(h, "eig_qr", st);
   for (int pass = 0; pass < passes; ++pass) {
     SG_BLAS(cublasSgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Y, n, Y, n, &zero, b.G, m));
     int* inf = b.info + std::min(b.n_info, b.cap_info - 3);
@@ -795,21 +797,25 @@ int filter_segment(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, co
   const float a1 = float(2.0 / cut), a2 = float(4.0 / cut), m1 = -1.f, m2 = -2.f, one = 1.f;
   float* prev = b.X;
   float* cur = b.P;
-  SG_CUDA(cudaMemcpyAsync(cur, prev, sizeof(float) * size_t(n) * m, cudaMemcpyDeviceToDevice, st));
-  SG_BLAS(filter_gemm(blas, n, m, &a1, A32, prev, &m1, cur));
   const int K = std::min(kTailCols, m);
-  tail_rq_kernel<<<K, 256, 0, st>>>(prev, cur, n, m, K, a1, b.R);
-  SG_LAUNCH_CHECK();
-  float hr[kTailCols];
-  SG_CUDA(cudaMemcpyAsync(hr, b.R, sizeof(float) * size_t(K), cudaMemcpyDeviceToHost, st));
-  for (int k = 2; k <= deg; ++k) {
-    // prev <- -prev - 2 cur, then prev <- (4/cut) A cur + prev
-    SG_BLAS(cublasSgeam(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, &m1, prev, n, &m2, cur, n, prev, n));
-    SG_BLAS(filter_gemm(blas, n, m, &a2, A32, cur, &one, prev));
-    std::swap(prev, cur);
+  {
+    sg::ProfScope prof_f(h, "eig_filter", st);
+    SG_CUDA(cudaMemcpyAsync(cur, prev, sizeof(float) * size_t(n) * m, cudaMemcpyDeviceToDevice, st));
+    SG_BLAS(filter_gemm(blas, n, m, &a1, A32, prev, &m1, cur));
+    tail_rq_kernel<<<K, 256, 0, st>>>(prev, cur, n, m, K, a1, b.R);
+    SG_LAUNCH_CHECK();
+    for (int k = 2; k <= deg; ++k) {
+      // prev <- -prev - 2 cur, then prev <- (4/cut) A cur + prev
+      SG_BLAS(cublasSgeam(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, &m1, prev, n, &m2, cur, n, prev, n));
+      SG_BLAS(filter_gemm(blas, n, m, &a2, A32, cur, &one, prev));
+      std::swap(prev, cur);
+    }
   }
   int rc = cholqr_f32(h, sol, blas, cur, n, m, b, qr_passes, st);
   if (rc) return rc;
+  // the tail quotients are read once the segment's work is queued
+  float hr[kTailCols];
+  SG_CUDA(cudaMemcpyAsync(hr, b.R, sizeof(float) * size_t(K), cudaMemcpyDeviceToHost, st));
   SG_CUDA(cudaStreamSynchronize(st));
   float mn = INFINITY;
   for (int k = 0; k < K; ++k) mn = std::isfinite(hr[k]) ? std::min(mn, hr[k]) : mn;
@@ -828,6 +834,7 @@ int filter_segment(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, co
 int ritz_f32(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, const float* A32, int n, int m, FilterBufs& b,
              int lwork_s, std::vector<float>& wh, bool vectors, cudaStream_t st) {
   const float one = 1.f, zero = 0.f;
+  sg::ProfScope prof(h, "eig_rr32", st);
   SG_BLAS(filter_gemm(blas, n, m, &one, A32, b.X, &zero, b.P));
   SG_BLAS(cublasSgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, b.X, n, b.P, n, &zero, b.G, m));
   int* inf = b.info + std::min(b.n_info, b.cap_info - 1);

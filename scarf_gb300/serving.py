@@ -59,6 +59,7 @@ class MapRequest:
     done: threading.Event = field(default_factory=threading.Event)
     ready: bool = True                 # CSR resident where the batches read it
     dev: Optional[tuple] = None        # device (indptr, indices, data)
+    t_admit: float = 0.0               # handed to the uploader
 
     def __post_init__(self):
         self.n_cells = len(self.indptr) - 1
@@ -278,6 +279,7 @@ class MappingServer:
                                     uploader=self._enqueue_upload)
         self.n_workers = int(n_workers)
         self.n_uploaders = max(1, int(n_uploaders))
+        self._upload_reserve = int(min(4 << 30, hbm_budget_bytes // (2 * self.n_uploaders)))
         self._threads: List[threading.Thread] = []
         self._rid = 0
         self._rid_lock = threading.Lock()
@@ -285,10 +287,11 @@ class MappingServer:
         self._up_cv = threading.Condition()
         self._stopping = False
         self.batches_run = 0
-        # (rows, seconds from batch taken to results on the host) per batch,
-        # (cells, seconds of the host-to-device copy) per request
+        # (rows, seconds from batch taken to results on the host) per batch;
+        # (cells, bytes, seconds queued for an uploader, seconds issuing the
+        # copies, seconds until they landed) per request
         self.batch_log: List[Tuple[int, float]] = []
-        self.upload_log: List[Tuple[int, float]] = []
+        self.upload_log: List[Tuple[int, int, float, float, float]] = []
 
     # -- client side ----------------------------------------------------------
     def submit(self, indptr, indices, data, arrival: Optional[float] = None) -> MapRequest:
@@ -327,6 +330,7 @@ class MappingServer:
 
     # -- uploader side --------------------------------------------------------
     def _enqueue_upload(self, req: MapRequest):
+        req.t_admit = time.perf_counter()
         with self._up_cv:
             heapq.heappush(self._up_heap, (req.n_cells, req.arrival, req.rid, req))
             self._up_cv.notify()
@@ -338,6 +342,12 @@ class MappingServer:
         import torch
         torch.cuda.set_device(self.device)
         stream = torch.cuda.Stream(self.device)
+        # reserve device memory for this uploader's copies in torch's cache, so
+        # that requests of new sizes split a cached segment instead of taking
+        # a fresh allocation while kernels run
+        with torch.cuda.stream(stream):
+            torch.empty(self._upload_reserve, dtype=torch.uint8, device=self.device)
+        stream.synchronize()
         while True:
             with self._up_cv:
                 while not self._up_heap and not self._stopping:
@@ -349,6 +359,7 @@ class MappingServer:
             try:
                 p0, p1 = int(req.indptr[0]), int(req.indptr[-1])
                 hs = [req.indptr, req.indices[p0:p1], req.data[p0:p1]]
+                nbytes = sum(int(a.nbytes) for a in hs)
                 if p1 == p0:  # keep the device pointers valid for an all-empty request
                     hs[1], hs[2] = np.zeros(1, np.int32), np.zeros(1, np.int32)
                 with torch.cuda.stream(stream), warnings.catch_warnings():
@@ -356,9 +367,11 @@ class MappingServer:
                     warnings.filterwarnings("ignore", message="The given NumPy array is not writable")
                     dev = tuple(torch.from_numpy(np.ascontiguousarray(h)).to(self.device, non_blocking=True)
                                 for h in hs)
+                t1 = time.perf_counter()
                 stream.synchronize()
                 req.dev = dev
-                self.upload_log.append((req.n_cells, time.perf_counter() - t0))
+                t2 = time.perf_counter()
+                self.upload_log.append((req.n_cells, nbytes, t0 - req.t_admit, t1 - t0, t2 - t1))
                 self.sched.mark_ready(req)
             except BaseException as e:  # surfaces in MapRequest.result()
                 self.sched.mark_ready(req, error=e)
@@ -389,6 +402,16 @@ class MappingServer:
                 [torch.zeros(1, dtype=torch.int32, device=self.device)]
         return h_ip.to(self.device, non_blocking=True), torch.cat(inds), torch.cat(dats), 0
 
+    def _run_batch(self, K, t_ip, t_ind, t_dat, off):
+        ref = self.ref
+        h = ref.nFeats
+        x = K.normalize_csr(t_ip, t_ind[off:], t_dat[off:], self.cmap, h, size_factor=self.size_factor,
+                            log_transform=self.log_transform, renormalize_subset=self.renorm,
+                            missing_mask=self.missing, fill_value=1.0)
+        s = K.project(x, ref._mu32, ref._sg32, ref._l32, ref.dims, n_cols=h)
+        return K.knn(s, ref.annIdx.scores, ref.dims, self.k, self_offset=-1, margin=ref.annIdx._margin(),
+                     precision=self.precision)
+
     def _worker(self):
         import torch
 
@@ -396,8 +419,15 @@ class MappingServer:
         torch.cuda.set_device(self.device)
         stream = torch.cuda.Stream(self.device)
         stage = _Staging()
-        ref = self.ref
-        h = ref.nFeats
+        # Size this worker's library scratch and torch's cache with one batch
+        # of the largest shape first: growing them later synchronises the
+        # whole device, which stalls every other stream (uploads included).
+        with torch.cuda.stream(stream):
+            rows = self.sched.max_rows
+            z = torch.zeros(rows + 1, dtype=torch.int64, device=self.device)
+            one = torch.zeros(1, dtype=torch.int32, device=self.device)
+            self._run_batch(K, z, one, one, 0)
+        stream.synchronize()
         while True:
             batch = self.sched.next_batch(timeout=0.05)
             if not batch:
@@ -408,12 +438,7 @@ class MappingServer:
             try:
                 with torch.cuda.stream(stream):
                     t_ip, t_ind, t_dat, off = self._batch_csr(batch, stage)
-                    x = K.normalize_csr(t_ip, t_ind[off:], t_dat[off:], self.cmap, h, size_factor=self.size_factor,
-                                        log_transform=self.log_transform, renormalize_subset=self.renorm,
-                                        missing_mask=self.missing, fill_value=1.0)
-                    s = K.project(x, ref._mu32, ref._sg32, ref._l32, ref.dims, n_cols=h)
-                    idx, dist, _ = K.knn(s, ref.annIdx.scores, ref.dims, self.k, self_offset=-1,
-                                         margin=ref.annIdx._margin(), precision=self.precision)
+                    idx, dist, _ = self._run_batch(K, t_ip, t_ind, t_dat, off)
                     hi = stage.get("oi", idx.numel(), idx.dtype).view(idx.shape)
                     hd = stage.get("od", dist.numel(), dist.dtype).view(dist.shape)
                     hi.copy_(idx, non_blocking=True)
