@@ -239,51 +239,50 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       thr = SHARE ? fminf(w, shared) : w;
     };
     // filter one chunk of 32 accumulator columns into the buffer; kRn: add
-    // |r|^2 here (not folded into the MMA); kMask: last tile, columns >= lim
-    // are past the last reference
-    auto process = [&](auto rn_tag, auto mask_tag, const uint32_t (&r)[32], int ch, int64_t r0, int lim) {
+    // |r|^2 here (not folded into the MMA). References past the last one
+    // carry an enormous key (a +inf norm, or a huge folded norm), so the last
+    // tile needs no mask. Four independent 8-key minima, then one branch per
+    // chunk: after the first tiles almost no chunk holds a passing key.
+    auto process = [&](auto rn_tag, const uint32_t (&r)[32], int ch, int64_t r0) {
       constexpr bool kRn = decltype(rn_tag)::value;
-      constexpr bool kMask = decltype(mask_tag)::value;
       const int cbase = int(r0) + ch * 32;
+      float kk[32];
 #pragma unroll
-      for (int j = 0; j < 32; j += 8) {
-        float kk[8];
+      for (int q = 0; q < 32; ++q) {
+        float key = __uint_as_float(r[q]);
+        if (kRn) key = fmaf(-2.f, key, my_rn[ch * 32 + q]);
+        kk[q] = key;
+      }
+      float m8[4];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          float key = __uint_as_float(r[j + q]);
-          if (kRn) key = fmaf(-2.f, key, my_rn[ch * 32 + j + q]);
-          if (kMask && ch * 32 + j + q >= lim) key = __int_as_float(0x7f800000);
-          kk[q] = key;
-        }
-        const float m = fminf(fminf(fminf(kk[0], kk[1]), fminf(kk[2], kk[3])),
-                              fminf(fminf(kk[4], kk[5]), fminf(kk[6], kk[7])));
-        if (m < thr) {
+      for (int g = 0; g < 4; ++g) {
+        const float* k8 = kk + 8 * g;
+        m8[g] = fminf(fminf(fminf(k8[0], k8[1]), fminf(k8[2], k8[3])), fminf(fminf(k8[4], k8[5]), fminf(k8[6], k8[7])));
+      }
+      if (fminf(fminf(m8[0], m8[1]), fminf(m8[2], m8[3])) < thr) {
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            if (kk[q] < thr) {
-              bk[cnt * SL] = kk[q];
-              bi[cnt * SL] = cbase + j + q;
-              ++cnt;
+        for (int g = 0; g < 4; ++g) {
+          if (m8[g] < thr) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              if (kk[8 * g + q] < thr) {
+                bk[cnt * SL] = kk[8 * g + q];
+                bi[cnt * SL] = cbase + 8 * g + q;
+                ++cnt;
+              }
             }
           }
         }
       }
     };
-    auto filter = [&](const uint32_t (&r)[32], int ch, int64_t r0, int lim) {
-      using T = std::true_type;
-      using F = std::false_type;
-      if (fold) {
-        if (lim < BN) process(F{}, T{}, r, ch, r0, lim);
-        else process(F{}, F{}, r, ch, r0, lim);
-      } else {
-        process(T{}, F{}, r, ch, r0, lim);  // padding references carry |r|^2 = +inf
-      }
+    auto filter = [&](const uint32_t (&r)[32], int ch, int64_t r0) {
+      if (fold) process(std::false_type{}, r, ch, r0);
+      else process(std::true_type{}, r, ch, r0);  // padding references carry |r|^2 = +inf
     };
     for (int t = 0; t < ntiles; ++t) {
       const int b = t & 1;
       const uint32_t aph = (t >> 1) & 1;
       const int64_t r0 = s_begin + int64_t(t) * BN;
-      const int lim = int(min(int64_t(BN), nr - r0));
       const bool use_rn = !fold;
       if (use_rn) {
         const float4* src = reinterpret_cast<const float4*>(rn + r0);
@@ -309,11 +308,11 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       for (int ch = 0; ch < NCH; ch += 2) {
         tmem_ld32(tbase + uint32_t((ch + 1) * 32), rb);
         if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
-        filter(ra, ch0 + ch, r0, lim);
+        filter(ra, ch0 + ch, r0);
         tmem_wait_ld(rb);
         if (ch + 2 < NCH) tmem_ld32(tbase + uint32_t((ch + 2) * 32), ra);
         if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
-        filter(rb, ch0 + ch + 1, r0, lim);
+        filter(rb, ch0 + ch + 1, r0);
         if (ch + 2 < NCH) tmem_wait_ld(ra);
       }
       tc_fence_before();
@@ -337,7 +336,8 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
 // BF16 operands, zero padded to 64 columns and n_pad rows.
 // refs: the rounded rows; with `fold`, columns d, d+1, d+2 carry |r_b|^2 split
 //   into three BF16 terms (hi, mid, lo), so that the product with the query's
-//   ones gives the norm to ~2^-24 relative; norms[] = |r_b|^2 (+inf for padding).
+//   ones gives the norm to ~2^-24 relative, and padding rows carry 1e38 there;
+//   norms[] = |r_b|^2 (+inf for padding).
 // queries: -2 * rounded rows (exact in BF16) and, with `fold`, ones in columns
 //   d..d+2. The accumulator is then |r|^2 - 2 q.r directly.
 __global__ void refs_bf16_kernel(const float* __restrict__ in, int64_t n, int d, int ld, int fold,
@@ -353,6 +353,7 @@ __global__ void refs_bf16_kernel(const float* __restrict__ in, int64_t n, int d,
     s = fmaf(bf, bf, s);
   }
   for (int c = d; c < BK; ++c) o[c] = __float2bfloat16_rn(0.f);
+  if (fold && r >= n) o[d] = __float2bfloat16_rn(1e38f);  // padding: a key no query keeps
   if (fold && r < n) {
     const __nv_bfloat16 hi = __float2bfloat16_rn(s);
     const float rem1 = s - __bfloat162float(hi);
