@@ -279,7 +279,8 @@ class MappingServer:
                                     uploader=self._enqueue_upload)
         self.n_workers = int(n_workers)
         self.n_uploaders = max(1, int(n_uploaders))
-        self._upload_reserve = int(min(4 << 30, hbm_budget_bytes // (2 * self.n_uploaders)))
+        # in-flight requests never exceed the admission budget
+        self._upload_reserve = int(min(16 << 30, hbm_budget_bytes // self.n_uploaders))
         self._threads: List[threading.Thread] = []
         self._rid = 0
         self._rid_lock = threading.Lock()
