@@ -724,6 +724,30 @@ __global__ void tail_rq_kernel(const float* __restrict__ X, const float* __restr
   if (threadIdx.x == 0) out[blockIdx.x] = (red[0][0] + red[1][0]) / (a1 * red[1][0]);
 }
 
+// v <- v / |v| and *rq = v^T y / v^T v (y = A v), one CTA
+__global__ void normalize_rq_kernel(float* __restrict__ v, const float* __restrict__ y, int n, float* __restrict__ rq) {
+  __shared__ float red[2][1024];
+  float a = 0.f, q = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    a = fmaf(v[i], v[i], a);
+    q = fmaf(v[i], y[i], q);
+  }
+  red[0][threadIdx.x] = a;
+  red[1][threadIdx.x] = q;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + o];
+      red[1][threadIdx.x] += red[1][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  const float nn = red[0][0];
+  if (threadIdx.x == 0) *rq = red[1][0] / nn;
+  const float inv = nn > 0.f ? rsqrtf(nn) : 1.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v[i] *= inv;
+}
+
 // reverse the column order of an m x m column-major matrix
 __global__ void reverse_cols_kernel(float* __restrict__ G, int m) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -900,7 +924,8 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
   const int cap_info = 128;
   const size_t need = sg::Carver::need(nn * 8) + sg::Carver::need(nn * 4) + 3 * sg::Carver::need(nm * 4) +
                       sg::Carver::need(size_t(m) * m * 4) + 2 * sg::Carver::need(size_t(m) * 4) +
-                      sg::Carver::need(kTailCols * 4) +
+                      sg::Carver::need(kTailCols * 4) + sg::Carver::need(nn * 4) + sg::Carver::need(size_t(n) * 12) +
+                      sg::Carver::need(8) +
                       3 * sg::Carver::need(np * 8) + 2 * sg::Carver::need(pp * 8) + sg::Carver::need(size_t(p) * 8) +
                       sg::Carver::need(size_t(p) * 8) + sg::Carver::need(16) + sg::Carver::need(cap_info * 4);
   int status;
@@ -917,6 +942,9 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
   b.W = cv.take<float>(size_t(m));
   b.D = cv.take<float>(size_t(m));
   b.R = cv.take<float>(size_t(kTailCols));
+  float* A32d = cv.take<float>(nn);       // the scatter with the locked pair deflated
+  float* lv = cv.take<float>(size_t(n) * 3);  // the locked vector and two recurrence buffers
+  float* lrq = cv.take<float>(2);
   double* Qd = cv.take<double>(np);
   double* Yd = cv.take<double>(np);
   double* Vd = cv.take<double>(np);
@@ -993,6 +1021,63 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
     // near the cut (many cells: a narrow Marchenko-Pastur bulk) gets more
     // segments, a well separated one fewer.
     double theta_c = double(th[size_t(m - std::min(m, n_comp))]);
+    // Lock a leading spike: when the largest Ritz value is far above the cut
+    // (t > 3) and 1.5 x the next, its growth alone would hold every segment to
+    // a low degree. Its vector is polished by one Chebyshev segment of its
+    // own (cut at the next Ritz value) and deflated from a copy of the
+    // scatter; the other m - 1 columns are filtered with the deflated
+    // operator, whose largest eigenvalue is then the next one.
+    const float* Aop = A32;
+    int L = 0, ma = m;
+    {
+      const double t1 = double(th[size_t(m - 1)]), t2 = double(th[size_t(m - 2)]);
+      if (2.0 * t1 / cut - 1.0 > 3.0 && t1 >= 1.5 * t2 && n_comp >= 2) L = 1;
+      if (L) {
+        const float one = 1.f, zero = 0.f, mtwo = -2.f, mone = -1.f;
+        float* v = lv;
+        float* y0 = lv + n;
+        float* y1 = lv + 2 * n;
+        SG_CUDA(cudaMemcpyAsync(v, b.X, sizeof(float) * size_t(n), cudaMemcpyDeviceToDevice, st));
+        const double cl = t2;  // a lower bound of the second eigenvalue
+        const int dl = std::min(24, int(std::ceil(std::acosh(1e8) / std::acosh(2.0 * t1 / cl - 1.0))));
+        const float a1 = float(2.0 / cl), a2 = float(4.0 / cl);
+        // y0 = v, y1 = (2/c) A v - v, y_{k+1} = (4/c) A y_k - 2 y_k - y_{k-1}
+        SG_CUDA(cudaMemcpyAsync(y0, v, sizeof(float) * size_t(n), cudaMemcpyDeviceToDevice, st));
+        SG_CUDA(cudaMemcpyAsync(y1, v, sizeof(float) * size_t(n), cudaMemcpyDeviceToDevice, st));
+        SG_BLAS(cublasSgemv(blas, CUBLAS_OP_N, n, n, &a1, A32, n, v, 1, &mone, y1, 1));
+        float* pr = y0;
+        float* cr = y1;
+        for (int k = 2; k <= dl; ++k) {
+          SG_BLAS(cublasSscal(blas, n, &mone, pr, 1));
+          SG_BLAS(cublasSaxpy(blas, n, &mtwo, cr, 1, pr, 1));
+          SG_BLAS(cublasSgemv(blas, CUBLAS_OP_N, n, n, &a2, A32, n, cr, 1, &one, pr, 1));
+          std::swap(pr, cr);
+        }
+        SG_CUDA(cudaMemcpyAsync(v, cr, sizeof(float) * size_t(n), cudaMemcpyDeviceToDevice, st));
+        normalize_rq_kernel<<<1, 1024, 0, st>>>(v, v, n, lrq + 1);  // unit length
+        SG_LAUNCH_CHECK();
+        SG_BLAS(cublasSgemv(blas, CUBLAS_OP_N, n, n, &one, A32, n, v, 1, &zero, y0, 1));
+        normalize_rq_kernel<<<1, 1024, 0, st>>>(v, y0, n, lrq);  // Rayleigh quotient of the unit vector
+        SG_LAUNCH_CHECK();
+        float hrq = 0.f;
+        SG_CUDA(cudaMemcpyAsync(&hrq, lrq, sizeof(float), cudaMemcpyDeviceToHost, st));
+        SG_CUDA(cudaStreamSynchronize(st));
+        if (!(hrq > 0.f) || !std::isfinite(hrq)) {
+          L = 0;
+        } else {
+          // deflated operator A - theta v v^T, and the active block X[:, 1:m]
+          SG_CUDA(cudaMemcpyAsync(A32d, A32, sizeof(float) * nn, cudaMemcpyDeviceToDevice, st));
+          const float mth = -hrq;
+          SG_BLAS(cublasSger(blas, n, n, &mth, v, 1, v, 1, A32d, n));
+          SG_CUDA(cudaMemcpyAsync(b.P, b.X + n, sizeof(float) * size_t(n) * (m - 1), cudaMemcpyDeviceToDevice, st));
+          std::swap(b.X, b.P);
+          Aop = A32d;
+          ma = m - 1;
+          theta_max = 1.05 * t2;
+          EIG_DBG("filter: locked theta=%g (RR1 %g), next %g, polish degree %d\n", double(hrq), t1, t2, dl);
+        }
+      }
+    }
     const double target = std::log(1e10);
     double gain = 0.0;
     int done = 0, segs = 0;
@@ -1006,7 +1091,7 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
       const double t_max = 2.0 * theta_max / cut - 1.0;
       const bool last = gain >= target;
       const int d = cheb_degree(t_max, last ? 1e2 : 1e5, 8);
-      rc = filter_segment(h, sol, blas, A32, n, m, d, cut, b, st, &rq, last && polish == 1 ? 2 : 1);
+      rc = filter_segment(h, sol, blas, Aop, n, ma, d, cut, b, st, &rq, last && polish == 1 ? 2 : 1);
       if (rc) return rc;
       if (!last) {
         gain += d * std::acosh(std::max(1.0, 2.0 * theta_c / cut - 1.0));
@@ -1018,15 +1103,16 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
         // below the block's tail: fresh Ritz values (of the orthonormalised
         // block, which they also put in descending order) give a higher,
         // still valid cap and a better rate estimate.
-        rc = cholqr_f32(h, sol, blas, b.X, n, m, b, 1, st);
+        rc = cholqr_f32(h, sol, blas, b.X, n, ma, b, 1, st);
         if (rc) return rc;
-        rc = ritz_f32(h, sol, blas, A32, n, m, b, lw_s, th, true, st);
+        rc = ritz_f32(h, sol, blas, Aop, n, ma, b, lw_s, th, true, st);
         if (rc) return rc;
         refreshed = true;
-        if (th[0] > 0.f && std::isfinite(th[size_t(m - 1)])) {
-          theta_w = std::max(theta_w, double(th[size_t(m - std::min(m, n_comp + 8))]));
-          theta_c = std::max(theta_c, double(th[size_t(m - std::min(m, n_comp))]));
-          theta_max = std::max(theta_max, 1.05 * double(th[size_t(m - 1)]));
+        if (th[0] > 0.f && std::isfinite(th[size_t(ma - 1)])) {
+          // pairs n_comp + 8 and n_comp overall are pairs n_comp + 8 - L and n_comp - L of the active block
+          theta_w = std::max(theta_w, double(th[size_t(ma - std::min(ma, n_comp + 8 - L))]));
+          theta_c = std::max(theta_c, double(th[size_t(ma - std::min(ma, n_comp - L))]));
+          theta_max = std::max(theta_max, 1.05 * double(th[size_t(ma - 1)]));
           cut_cap = 0.99 * theta_w;
         }
         EIG_DBG("filter: refresh theta_c=%g theta_w=%g\n", theta_c, theta_w);
@@ -1034,6 +1120,15 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
       if (std::isfinite(rq)) cut = std::min(cut_cap, std::max(cut, double(rq)));
       if (last) ++polish;
       if (done >= 240 && !last) gain = target;  // degree cap
+    }
+    if (L) {
+      // the locked vector back in front of the active block, orthonormalised
+      // together, for the Rayleigh-Ritz step on the undeflated scatter
+      SG_CUDA(cudaMemcpyAsync(b.P, lv, sizeof(float) * size_t(n), cudaMemcpyDeviceToDevice, st));
+      SG_CUDA(cudaMemcpyAsync(b.P + n, b.X, sizeof(float) * size_t(n) * ma, cudaMemcpyDeviceToDevice, st));
+      std::swap(b.X, b.P);
+      rc = cholqr_f32(h, sol, blas, b.X, n, m, b, 2, st);
+      if (rc) return rc;
     }
     rc = ritz_f32(h, sol, blas, A32, n, m, b, lw_s, th, true, st);
     if (rc) return rc;
