@@ -608,7 +608,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--mode", default="full", choices=["full", "step", "serve", "knn"],
+    ap.add_argument("--mode", default="full", choices=["full", "step", "serve", "knn", "union", "batched"],
                     help="step: warm-up steps then one make_graph step and nothing else (for profilers); "
                          "serve: the mapping service's latency under a Poisson request stream")
     ap.add_argument("--form", default="precision", choices=["precision", "plain"], help="form used by --mode step")
@@ -625,6 +625,10 @@ def main():
         run_serve(args)
     elif args.mode == "knn":
         run_knn(args)
+    elif args.mode == "union":
+        run_union(args, cfg)
+    elif args.mode == "batched":
+        run_batched(args)
     else:
         run_gb300(args, cfg)
 
@@ -753,6 +757,89 @@ def run_knn(args):
     K.profile(False)
     print(json.dumps({"mode": "knn", "queries": int(q.shape[0]), "refs": n, "knn_tc_ms": round(t, 3),
                       "rerank_ms": round(t2, 3), "missed": int(nm.item())}))
+
+
+BATCHED = dict(name="C5: 256 independent samples of log-uniform 500-20,000 cells (20,000 genes NB, 8 clusters, "
+                     "library sizes around 3,000: the C1 generator), 2,000 HVGs, 30 PCs, k=15; kNN + smoothing + "
+                     "fuzzy union per sample",
+               n_samples=256, lo=500, hi=20_000, n_genes=20_000, n_clusters=8, n_hvg=2000, dims=30, k=15)
+
+
+def run_batched(args):
+    """Cells/s of many small graphs: the precision form through
+    pipeline.make_graphs (4 streams) against the plain form sample by sample."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from scarf_gb300 import pipeline, synth
+    c = BATCHED
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(11)
+    sizes = np.exp(rng.uniform(np.log(c["lo"]), np.log(c["hi"]), c["n_samples"])).astype(int)
+    total = int(sizes.sum())
+    pool = synth.nb_counts(total, c["n_genes"], c["n_clusters"], SEED, device=dev)
+    feat = synth.select_hvgs(pool, c["n_hvg"])
+    samples, a = [], 0
+    for s_ in sizes:
+        p0, p1 = int(pool.indptr[a]), int(pool.indptr[a + s_])
+        samples.append((torch.from_numpy(pool.indptr[a:a + s_ + 1] - p0).to(dev),
+                        torch.from_numpy(pool.indices[p0:p1]).to(dev), torch.from_numpy(pool.data[p0:p1]).to(dev)))
+        a += s_
+    del pool
+    kw = dict(keep_x=False, batch_size=BATCH)
+    pipeline.make_graphs(samples[:8], c["n_genes"], feat, c["dims"], c["k"], **kw)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = pipeline.make_graphs(samples, c["n_genes"], feat, c["dims"], c["k"], **kw)
+    torch.cuda.synchronize()
+    t_prec = time.perf_counter() - t0
+    rec = float(np.mean([graph_check(g, BATCH, n_sample=200)[0] for g, _ in res[::16]]))
+    # the plain form, one sample after another on one stream
+    for smp in samples[:4]:
+        pipeline.make_graph(*smp, c["n_genes"], feat, c["dims"], c["k"], precision="plain", **kw)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for smp in samples:
+        g = pipeline.make_graph(*smp, c["n_genes"], feat, c["dims"], c["k"], precision="plain", **kw)
+        K_union(g)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    print(json.dumps({"metric": "batched make_graph + union cells/s", "value": round(total / t_prec, 1),
+                      "unit": "cells/s", "higher_is_better": True, "samples": len(samples), "cells": total,
+                      "seconds": round(t_prec, 3), "plain_sequential_seconds": round(t_plain, 3),
+                      "speedup_vs_plain_sequential": round(t_plain / t_prec, 3), "sampled_recall_at_k": round(rec, 5),
+                      "data": "synthetic", "config": {"workload": c["name"], "streams": 4}}), flush=True)
+
+
+def K_union(g):
+    from scarf_gb300 import kernels as K
+    return K.fuzzy_union(g.edges, g.weights, g.n_cells, g.k)
+
+
+def run_union(args, cfg):
+    """The fuzzy union (load_graph(symmetric=True)) of one precision graph of
+    the config, W warm-up calls and one more (profiling case)."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from scarf_gb300 import kernels as K
+    from scarf_gb300 import pipeline
+    dev = torch.device("cuda", 0)
+    csr, feat = make_input(cfg, dev)
+    ip, ind, dat = (torch.from_numpy(a).to(dev) for a in (csr.indptr, csr.indices, csr.data))
+    res = pipeline.make_graph(ip, ind, dat, csr.n_genes, feat, cfg["dims"], cfg["k"], batch_size=BATCH,
+                              precision="precision", keep_x=False)
+    del ip, ind, dat
+    for _ in range(args.warmup):
+        K.fuzzy_union(res.edges, res.weights, res.n_cells, res.k)
+    K.profile(True)
+    K.profile_reset()
+    indptr, _, _ = K.fuzzy_union(res.edges, res.weights, res.n_cells, res.k)
+    torch.cuda.synchronize()
+    t, _ = K.profile_query("union")
+    K.profile(False)
+    print(json.dumps({"mode": "union", "config": args.config, "union_ms": round(t, 3),
+                      "nnz": int(indptr[-1].item())}))
 
 
 def run_step(args, cfg):

@@ -64,6 +64,16 @@ size_t sg_workspace_bytes(const sg_handle* h);
  * events. */
 unsigned long long sg_kernel_launches(void);
 int sg_profile(sg_handle* h, int enable);
+
+/* Autotuning (no reference counterpart): with enable != 0, the first
+ * precision-form sg_knn of a shape bucket (log2 of the query rows, log2 of the
+ * reference rows, d, candidate-list length) with at least 1e9 query-reference
+ * pairs times three reference split counts and keeps the fastest for later
+ * calls of that bucket on this handle. Off by default: the first call of a
+ * bucket then costs about three calls. sg_knn_last_splits returns the split
+ * count of the last precision-form sg_knn. */
+int sg_set_autotune(sg_handle* h, int enable);
+int sg_knn_last_splits(const sg_handle* h);
 int sg_profile_reset(sg_handle* h);
 int sg_profile_query(sg_handle* h, const char* name, double* total_ms, long long* count);
 

@@ -131,6 +131,14 @@ size_t sg_workspace_bytes(const sg_handle* h) { return h ? h->ws_bytes : 0; }
 
 unsigned long long sg_kernel_launches(void) { return g_launches.load(); }
 
+int sg_set_autotune(sg_handle* h, int enable) {
+  if (!h) return sg::fail(SG_ERR_ARG, "null sg_handle");
+  h->autotune = enable != 0;
+  return SG_OK;
+}
+
+int sg_knn_last_splits(const sg_handle* h) { return h ? h->last_knn_splits : 0; }
+
 int sg_profile(sg_handle* h, int enable) {
   if (!h) return sg::fail(SG_ERR_ARG, "null sg_handle");
   cudaSetDevice(h->device);

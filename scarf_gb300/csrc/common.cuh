@@ -25,6 +25,14 @@ struct sg_handle {
   // max relative FP64 residual of the last sg_pca_basis_filter call
   // (NaN: it used the dense route; infinity: it fell back to it)
   double eig_resid = std::numeric_limits<double>::quiet_NaN();
+  // kNN split autotuning (off unless sg_set_autotune(h, 1)): the chosen split
+  // count per (log2 query rows, log2 reference rows, d, list length) bucket
+  bool autotune = false;
+  struct KnnTune {
+    int qb, rb, d, kc, nsplit;
+  };
+  std::vector<KnnTune> knn_tune;
+  int last_knn_splits = 0;
   // kernel timing (off unless sg_profile(h, 1)): events around named launches
   bool prof = false;
   struct ProfRec {

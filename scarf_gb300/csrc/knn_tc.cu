@@ -408,11 +408,26 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   const int64_t nr_pad = sg::ceil_div(nr, BN) * BN;
   if (nr_pad >= (int64_t(1) << 31) || nq_pad >= (int64_t(1) << 31)) return sg::fail(SG_ERR_ARG, "sg_knn: too many rows");
   const int qtiles = int(nq_pad / BM);
-  int nsplit = std::max<int>(1, int(std::lround(double(h->sm_count) * 8 / qtiles)));
-  nsplit = int(std::min<int64_t>(nsplit, std::max<int64_t>(1, nr_pad / (BN * 4))));
-  nsplit = std::min(nsplit, 256);
+  // reference splits per query tile: the heuristic fills ~8 CTAs per SM
+  auto splits_for = [&](int want) {
+    int ns = std::max(1, want);
+    ns = int(std::min<int64_t>(ns, std::max<int64_t>(1, nr_pad / (BN * 4))));
+    ns = std::min(ns, 256);
+    const int64_t rps_ = sg::ceil_div(sg::ceil_div(nr, ns), BN) * BN;
+    return int(sg::ceil_div(nr, rps_));
+  };
+  const int ns0 = splits_for(int(std::lround(double(h->sm_count) * 8 / qtiles)));
+  auto ilog2 = [](int64_t v) {
+    int r = 0;
+    while ((int64_t(1) << (r + 1)) <= v) ++r;
+    return r;
+  };
+  const int qb = ilog2(nq_pad), rb = ilog2(nr_pad);
+  int tuned = 0;
+  for (const auto& e : h->knn_tune)
+    if (e.qb == qb && e.rb == rb && e.d == d && e.kc == kc) tuned = e.nsplit;
+  auto run = [&](int nsplit) -> int {
   const int64_t rps = sg::ceil_div(sg::ceil_div(nr, nsplit), BN) * BN;
-  nsplit = int(sg::ceil_div(nr, rps));
   const int fold = d <= BK - 3 ? 1 : 0;
   const size_t need = sg::Carver::need(size_t(nr_pad) * BK * 2) + sg::Carver::need(size_t(nr_pad) * 4) +
                       sg::Carver::need(size_t(nq_pad) * BK * 2) +
@@ -454,6 +469,41 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   SG_CUDA(cudaStreamSynchronize(st));
   if (herr) return sg::fail(SG_ERR_TIMEOUT, "sg_knn: a tensor-core pipeline wait expired (stage %d)", herr);
   sg::ProfScope prof(h, "rerank", st);
+  h->last_knn_splits = nsplit;
   return sg_rerank(queries, refs, d, ld, nq, cand, nsplit * HALVES, kc, nq_pad, kq, k, self_offset, idx_out, dist_out,
                    nmiss, st);
+  };
+  if (tuned) return run(tuned);
+  if (!h->autotune || double(nq) * double(nr) < 1e9) return run(ns0);
+  // Autotune the split count for this (query, reference, d, list) bucket:
+  // time the heuristic, half and double of it (kernel + re-rank) once and keep
+  // the fastest. Every candidate returns the same exact top k; the last run's
+  // outputs stand.
+  std::vector<int> cands{ns0};
+  for (int c : {splits_for(std::max(1, ns0 / 2)), splits_for(ns0 * 2)})
+    if (std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
+  cudaEvent_t e0, e1;
+  SG_CUDA(cudaEventCreate(&e0));
+  SG_CUDA(cudaEventCreate(&e1));
+  int best = ns0;
+  float best_ms = INFINITY;
+  int rc = SG_OK;
+  for (int c : cands) {
+    SG_CUDA(cudaEventRecord(e0, st));
+    rc = run(c);
+    if (rc) break;
+    SG_CUDA(cudaEventRecord(e1, st));
+    SG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    SG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  h->knn_tune.push_back({qb, rb, d, kc, best});
+  return SG_OK;
 }

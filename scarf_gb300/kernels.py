@@ -191,6 +191,16 @@ def pca_basis(cov: torch.Tensor, zsum: Optional[torch.Tensor], n_used: int, n_co
     return comps, evals, evr, l32
 
 
+def set_autotune(enable: bool, device: Optional[int] = None) -> None:
+    """Autotune the precision kNN's reference split count per shape bucket on
+    this thread's handle (see sg_set_autotune)."""
+    L.check(L.load().sg_set_autotune(handle(device).ptr, int(bool(enable))))
+
+
+def knn_last_splits(device: Optional[int] = None) -> int:
+    return int(L.load().sg_knn_last_splits(handle(device).ptr))
+
+
 def filter_residual(device: Optional[int] = None) -> float:
     """Max relative FP64 residual of the wanted pairs of the last
     ``pca_basis(eigh='filter')`` on this thread's handle (NaN: dense route for

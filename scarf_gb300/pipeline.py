@@ -147,7 +147,7 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k:
                log_transform: bool = True, renormalize_subset: bool = True, n_counts=None,
                use_for_pca: Optional[np.ndarray] = None, chunk_cells: Optional[int] = None,
                smooth: bool = True, keep_x: bool = True, cov_form: Optional[str] = None,
-               eigh: Optional[str] = None, device="cuda") -> GraphResult:
+               eigh: Optional[str] = None, autotune: bool = True, device="cuda") -> GraphResult:
     """The whole path on the device; returns device tensors.
 
     ``precision`` selects the form: "plain" (FP32 scatter, FP32 kNN, full FP64
@@ -179,6 +179,7 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k:
     scores = K.project(x, mu32, sigma32, l32, dims, n_cols=h)
     if margin is None:
         margin = PRECISION_MARGIN if precision == "precision" else PLAIN_MARGIN
+    K.set_autotune(autotune, dev.index)
     idx, dist, nm = K.knn(scores, scores, dims, k, self_offset=0, margin=margin, precision=precision)
     res = GraphResult(n_cells=n, n_feats=h, dims=dims, k=k, x=x if keep_x else None, mu=mu, sigma=sigma,
                       mu32=mu32, sigma32=sigma32, components=comps, loadings32=l32, evals=evals, evr=evr,
@@ -186,3 +187,37 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k:
     if smooth:
         res.edges, res.weights = K.smooth(idx, dist, local_connectivity, bandwidth, batch_size)
     return res
+
+
+def make_graphs(samples, n_genes: int, feat_idx, dims: int = 30, k: int = 15, *, precision: str = "precision",
+                union: bool = True, n_streams: int = 4, device="cuda", **kw) -> list:
+    """Graphs of many independent samples (config C5: hundreds of samples of
+    500-20,000 cells). ``samples`` is a sequence of ``(indptr, indices, data)``
+    CSR triples sharing the gene space and the feature list. Each sample runs
+    ``make_graph`` (and, with ``union``, the fuzzy union of its graph) on one
+    of ``n_streams`` worker threads, each with its own CUDA stream and library
+    handle, so that the launches of small samples overlap on the device.
+    Returns ``[(GraphResult, (indptr, indices, data) or None), ...]`` in
+    sample order; the result of a sample does not depend on the others."""
+    import concurrent.futures as cf
+    dev = torch.device(device)
+    out = [None] * len(samples)
+    streams = [torch.cuda.Stream(dev) for _ in range(max(1, n_streams))]
+    local = {}
+
+    def run(i):
+        import threading
+        tid = threading.get_ident()
+        if tid not in local:
+            local[tid] = streams[len(local) % len(streams)]
+        st = local[tid]
+        ip, ind, dat = samples[i]
+        with torch.cuda.stream(st):
+            g = make_graph(ip, ind, dat, n_genes, feat_idx, dims, k, precision=precision, device=dev, **kw)
+            u = K.fuzzy_union(g.edges, g.weights, g.n_cells, g.k) if union else None
+        st.synchronize()
+        out[i] = (g, u)
+
+    with cf.ThreadPoolExecutor(max_workers=len(streams)) as ex:
+        list(ex.map(run, range(len(samples))))
+    return out

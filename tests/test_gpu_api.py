@@ -146,3 +146,27 @@ def test_mapping_server_rejects_over_budget(ds):
         r = srv.submit(indptr[:101] - indptr[0], indices[: indptr[100]], data[: indptr[100]])
         with pytest.raises(MemoryError):
             r.result(timeout=10)
+
+
+def test_make_graphs_equals_one_by_one():
+    # many small graphs on 3 streams give what each gives alone
+    from helpers import small_counts, top_var_genes
+    from scarf_gb300 import pipeline
+    indptr, indices, data, G, _ = small_counts()
+    feat = top_var_genes(indptr, indices, data, G, 300)
+    cuts = [0, 300, 700, 1500]
+    samples = []
+    for a, b in zip(cuts[:-1], cuts[1:]):
+        p0, p1 = int(indptr[a]), int(indptr[b])
+        samples.append((torch.from_numpy((indptr[a:b + 1] - p0).astype(np.int64)).cuda(),
+                        torch.from_numpy(indices[p0:p1].astype(np.int32)).cuda(),
+                        torch.from_numpy(data[p0:p1].astype(np.int32)).cuda()))
+    many = pipeline.make_graphs(samples, G, feat, 20, 10, n_streams=3)
+    for (g, u), smp in zip(many, samples):
+        one = pipeline.make_graph(*smp, G, feat, 20, 10, precision="precision")
+        assert np.array_equal(g.indices.cpu().numpy(), one.indices.cpu().numpy())
+        assert np.array_equal(g.weights.cpu().numpy(), one.weights.cpu().numpy())
+        ui, uj, uv = (t.cpu().numpy() for t in u)
+        from scarf_gb300 import kernels as K
+        oi, oj, ov = (t.cpu().numpy() for t in K.fuzzy_union(one.edges, one.weights, one.n_cells, one.k))
+        assert np.array_equal(ui, oi) and np.array_equal(uj, oj) and np.array_equal(uv, ov)
