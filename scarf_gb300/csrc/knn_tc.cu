@@ -51,6 +51,13 @@ __host__ __device__ constexpr size_t smem_bytes(int) {
 // Instruction descriptor, kind::f16: D F32, A/B BF16, both K-major, N, M.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
 
+// min of three floats in one PTX instruction (sm_100 and later)
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // Order-preserving map of a float to uint32 (for atomicMin across CTAs) and back.
 __device__ __forceinline__ uint32_t key_bits(float f) {
   const uint32_t u = __float_as_uint(f);
@@ -257,9 +264,9 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
 #pragma unroll
       for (int g = 0; g < 4; ++g) {
         const float* k8 = kk + 8 * g;
-        m8[g] = fminf(fminf(fminf(k8[0], k8[1]), fminf(k8[2], k8[3])), fminf(fminf(k8[4], k8[5]), fminf(k8[6], k8[7])));
+        m8[g] = fmin3(fmin3(k8[0], k8[1], k8[2]), fmin3(k8[3], k8[4], k8[5]), fminf(k8[6], k8[7]));
       }
-      if (fminf(fminf(m8[0], m8[1]), fminf(m8[2], m8[3])) < thr) {
+      if (fminf(fmin3(m8[0], m8[1], m8[2]), m8[3]) < thr) {
 #pragma unroll
         for (int g = 0; g < 4; ++g) {
           if (m8[g] < thr) {
