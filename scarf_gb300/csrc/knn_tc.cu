@@ -1,16 +1,20 @@
 // a6/a7 precision form: BF16 distance tiles on the tcgen05 tensor cores.
 //
-// One CTA owns 128 queries (one TMEM lane each) and a range of reference rows.
-//   warp 0      TMA producer: the BF16 query tile once, then 256-row reference
+// One CTA owns 256 queries (two 128-row query tiles, one TMEM lane per query
+// of each) and a range of reference rows.
+//   warp 0      TMA producer: the BF16 query tiles once, then 128-row reference
 //               tiles into a 4-stage shared-memory ring (128B swizzle, K = 64).
-//   warp 1      MMA issuer (one thread): D[128x256] = Q . R^T as four
-//               tcgen05.mma kind::f16 K=16 steps into one of two TMEM
-//               accumulators (2 x 256 columns), committed to the ring's empty
-//               barrier and to the accumulator's full barrier.
-//   warps 2-5   epilogue: tcgen05.ld 32 columns at a time, ranking key
-//               |r|^2 - 2 q.r, threshold test, register top-KC insertion; the
-//               accumulator is handed back as soon as it has been read, so the
-//               MMA of tile t+1 overlaps the epilogue of tile t.
+//   warp 1      MMA issuer (one thread): per reference tile, D0 = Q0 . R^T and
+//               D1 = Q1 . R^T (128 x 128 each) as tcgen05.mma kind::f16 K=16
+//               steps into one of two TMEM accumulator pairs (2 x 256 columns),
+//               committed to the ring's empty barrier and to the accumulator's
+//               full barrier. Each reference tile read from L2 feeds 256 queries.
+//   warps 2-9   epilogue, two per TMEM lane quarter (one per query tile): each
+//               reads its 32 queries' 128 columns 32 at a time with tcgen05.ld,
+//               takes the ranking key |r|^2 - 2 q.r, tests it against the
+//               query's current threshold and keeps one register top-KC list
+//               per query; the accumulator is handed back as soon as it has been
+//               read, so the MMAs of tile t+1 overlap the epilogue of tile t.
 // Every mbarrier wait is bounded: on expiry the kernel raises an error flag,
 // drains its own TMA copies and MMAs (again bounded), frees TMEM and returns.
 // The candidates are re-ranked exactly in FP32 by knn.cu.
@@ -28,25 +32,26 @@ namespace {
 
 using namespace tc;
 
-constexpr int BM = 128;
-constexpr int BN = 256;
+constexpr int BM = 128;           // queries per tile (TMEM lanes)
+constexpr int QT = 2;             // query tiles per CTA
+constexpr int BQ = BM * QT;       // queries per CTA
+constexpr int BN = 128;           // references per tile
 constexpr int BK = 64;
-constexpr int STAGES = 3;
-constexpr uint32_t A_BYTES = BM * BK * 2;
+constexpr int STAGES = 4;
+constexpr uint32_t A_BYTES = BQ * BK * 2;
+constexpr uint32_t A_TILE_BYTES = BM * BK * 2;
 constexpr uint32_t B_BYTES = BN * BK * 2;
 constexpr uint32_t TMEM_COLS = 512;
-// 8 epilogue warps: two per TMEM lane quarter, each filtering one half of
-// every 256-column tile for its 32 rows with its own candidate list, so that
-// each scheduler has a second warp to issue while the other waits
-constexpr int EPI_WARPS = 8;
-constexpr int HALVES = EPI_WARPS / 4;
-constexpr int HCOLS = BN / HALVES;  // accumulator columns per epilogue warp
+constexpr uint32_t ACC_COLS = QT * BN;  // one accumulator pair
+constexpr int EPI_WARPS = 4 * QT;
 constexpr int THREADS = 64 + 32 * EPI_WARPS;
-constexpr int BUF = 48;  // candidate buffer slots per (query row, half)
+constexpr int BUF = 48;  // candidate buffer slots per query
 __host__ __device__ constexpr size_t smem_bytes(int) {
   return 1024 /*align*/ + A_BYTES + STAGES * B_BYTES + 256 /*barriers*/ + EPI_WARPS * BN * 4 /*rn*/ +
-         size_t(BUF) * BM * HALVES * 8 /*buffers*/ + size_t(HALVES) * BM * 4 /*published bounds*/;
+         size_t(BUF) * BQ * 8 /*buffers*/;
 }
+static_assert(smem_bytes(0) <= 227 * 1024, "shared memory budget");
+static_assert(2 * ACC_COLS <= TMEM_COLS, "two accumulator pairs");
 
 // Instruction descriptor, kind::f16: D F32, A/B BF16, both K-major, N, M.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
@@ -79,29 +84,30 @@ struct TopK {
     }
   }
   __device__ __forceinline__ float worst() const { return d[KC - 1]; }
+  // Sorted insert of v (< worst()) after any equal keys. Slot j changes when
+  // d[j] > v and then takes slot j-1's entry when that one is also above v,
+  // else v: every slot is decided from the old list alone, with no chain
+  // between slots.
   __device__ __forceinline__ void insert(float v, int vi) {
-    bool placed = false;
 #pragma unroll
     for (int j = KC - 1; j >= 1; --j) {
-      const bool sh = d[j - 1] > v;
-      const float nd = sh ? d[j - 1] : v;
-      const int ni = sh ? i[j - 1] : vi;
-      if (!placed) {
-        d[j] = nd;
-        i[j] = ni;
-      }
-      placed = placed || !sh;
+      const bool gt = d[j] > v;
+      const bool up = d[j - 1] > v;
+      const float nd = up ? d[j - 1] : v;
+      const int ni = up ? i[j - 1] : vi;
+      d[j] = gt ? nd : d[j];
+      i[j] = gt ? ni : i[j];
     }
-    if (!placed) {
+    if (d[0] > v) {
       d[0] = v;
       i[0] = vi;
     }
   }
 };
 
-// SHARE: the lists of a query share their worst keys (worth it when the
-// references are split over several CTAs; with one split the extra state
-// costs more than the candidates it saves)
+// SHARE: the lists of a query in different CTAs (reference splits) share
+// their worst keys through `qbound` (worth it with several splits; with one
+// the extra state costs more than the candidates it saves)
 template <int KC, bool SHARE>
 __global__ void __launch_bounds__(THREADS, 1)
 knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
@@ -120,17 +126,15 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   uint64_t* a_full = acc_empty + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(a_full + 1);
   float* rn_s = reinterpret_cast<float*>(sm + A_BYTES + STAGES * B_BYTES + 256);
-  float* bufk = rn_s + EPI_WARPS * BN;                               // [BUF][HALVES * BM]
-  int* bufi = reinterpret_cast<int*>(bufk + BUF * BM * HALVES);      // [BUF][HALVES * BM]
-  float* pub = reinterpret_cast<float*>(bufi + BUF * BM * HALVES);   // [HALVES][BM] each list's worst
+  float* bufk = rn_s + EPI_WARPS * BN;                         // [BUF][BQ]
+  int* bufi = reinterpret_cast<int*>(bufk + BUF * BQ);         // [BUF][BQ]
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t q0 = int64_t(blockIdx.x) * BM;
+  const int64_t q0 = int64_t(blockIdx.x) * BQ;
   const int64_t s_begin = int64_t(blockIdx.y) * rps;
   const int64_t s_end = min(nr, s_begin + rps);
   const int ntiles = int((s_end - s_begin + BN - 1) / BN);
 
-  for (int i = threadIdx.x; i < HALVES * BM; i += blockDim.x) pub[i] = __int_as_float(0x7f800000);
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full[s], 1);
@@ -181,7 +185,8 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       int issued = 0;
       if (mbar_wait(a_full, 0, err, 2)) {
         tc_fence_after();
-        const uint64_t adesc = smem_desc_sw128(su32(sA));
+        const uint64_t adesc0 = smem_desc_sw128(su32(sA));
+        const uint64_t adesc1 = smem_desc_sw128(su32(sA + A_TILE_BYTES));
         for (int t = 0; t < ntiles; ++t) {
           const int s = t % STAGES;
           const uint32_t ph = (t / STAGES) & 1;
@@ -191,10 +196,13 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
           if (!mbar_wait(&full[s], ph, err, 4)) break;
           tc_fence_after();
           const uint64_t bdesc = smem_desc_sw128(su32(sB + s * B_BYTES));
+          const uint32_t d0 = tmem + uint32_t(b) * ACC_COLS;
 #pragma unroll
-          for (int kk = 0; kk < BK / 16; ++kk)
-            mma_bf16(tmem + uint32_t(b * BN), adesc + uint64_t(2 * kk), bdesc + uint64_t(2 * kk), kIdesc,
+          for (int kk = 0; kk < BK / 16; ++kk) {
+            mma_bf16(d0, adesc0 + uint64_t(2 * kk), bdesc + uint64_t(2 * kk), kIdesc, kk > 0 ? 1u : 0u);
+            mma_bf16(d0 + uint32_t(BN), adesc1 + uint64_t(2 * kk), bdesc + uint64_t(2 * kk), kIdesc,
                      kk > 0 ? 1u : 0u);
+          }
           mma_commit(&empty[s]);
           mma_commit(&acc_full[b]);
           ++issued;
@@ -208,39 +216,36 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       }
     }
   } else {
-    const int quarter = warp & 3;  // TMEM lanes [32*quarter, 32*quarter+32) are this warp's
-    const int half = (warp - 2) / 4;  // accumulator columns [HCOLS*half, HCOLS*half + HCOLS)
-    const int row = quarter * 32 + lane;
+    const int quarter = warp & 3;      // TMEM lanes [32*quarter, 32*quarter+32) are this warp's
+    const int sel = (warp - 2) >> 2;   // query tile: accumulator columns [BN*sel, BN*sel + BN)
+    const int row = sel * BM + quarter * 32 + lane;  // query of this thread within the CTA
     float* my_rn = rn_s + (warp - 2) * BN;
-    float* bk = bufk + half * BM + row;  // slot s of this (row, half)'s buffer: bk[s * HALVES * BM]
-    int* bi = bufi + half * BM + row;
-    constexpr int SL = HALVES * BM;      // buffer slot stride
+    float* bk = bufk + row;  // slot s of this query's buffer: bk[s * BQ]
+    int* bi = bufi + row;
     TopK<KC> top;
     top.init();
-    // Every list of a query (its two halves here, its reference splits in
-    // other CTAs) holds keys of that query, so each full list's worst key
-    // bounds the query's final KC-th key from above: a candidate at or above
-    // the smallest of them cannot make the query's top KC. The halves share
-    // their worst keys through shared memory, the splits through `qbound`
-    // (atomicMin on an order-preserving encoding); both only decrease, so a
-    // stale value is still a valid bound.
+    // Every list of a query (its reference splits in other CTAs) holds keys of
+    // that query, so each full list's worst key bounds the query's final
+    // KC-th key from above: a candidate at or above the smallest of them
+    // cannot make the query's top KC. The splits share their worst keys
+    // through `qbound` (atomicMin on an order-preserving encoding); it only
+    // decreases, so a stale value is still a valid bound.
     unsigned* qb = qbound + q0 + row;
-    float* my_pub = pub + half * BM + row;
-    const float* other_pub = pub + (half ^ 1) * BM + row;
     float shared = __int_as_float(0x7f800000);  // smallest worst key of the other lists
+    float published = shared;
     float thr = shared;
     int cnt = 0;
     // merge the buffered candidates into the sorted register list, then
     // publish the list's worst key
     auto compact = [&]() {
       for (int s2 = 0; s2 < cnt; ++s2) {
-        const float v = bk[s2 * SL];
-        if (v < top.worst() && (!SHARE || v < shared)) top.insert(v, bi[s2 * SL]);
+        const float v = bk[s2 * BQ];
+        if (v < top.worst() && (!SHARE || v < shared)) top.insert(v, bi[s2 * BQ]);
       }
       cnt = 0;
       const float w = top.worst();
-      if (SHARE && w < *my_pub) {
-        *my_pub = w;
+      if (SHARE && w < published) {
+        published = w;
         atomicMin(qb, key_bits(w));
       }
       thr = SHARE ? fminf(w, shared) : w;
@@ -273,8 +278,8 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
               if (kk[8 * g + q] < thr) {
-                bk[cnt * SL] = kk[8 * g + q];
-                bi[cnt * SL] = cbase + 8 * g + q;
+                bk[cnt * BQ] = kk[8 * g + q];
+                bi[cnt * BQ] = cbase + 8 * g + q;
                 ++cnt;
               }
             }
@@ -282,54 +287,55 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
         }
       }
     };
-    auto filter = [&](const uint32_t (&r)[32], int ch, int64_t r0) {
-      if (fold) process(std::false_type{}, r, ch, r0);
-      else process(std::true_type{}, r, ch, r0);  // padding references carry |r|^2 = +inf
-    };
-    for (int t = 0; t < ntiles; ++t) {
-      const int b = t & 1;
-      const uint32_t aph = (t >> 1) & 1;
-      const int64_t r0 = s_begin + int64_t(t) * BN;
-      const bool use_rn = !fold;
-      if (use_rn) {
-        const float4* src = reinterpret_cast<const float4*>(rn + r0);
-        reinterpret_cast<float4*>(my_rn)[lane * 2] = __ldg(src + lane * 2);
-        reinterpret_cast<float4*>(my_rn)[lane * 2 + 1] = __ldg(src + lane * 2 + 1);
-      }
-      if (SHARE) {
-        shared = fminf(shared, fminf(*other_pub, bits_key(__ldcg(qb))));
-        thr = fminf(thr, shared);
-      }
-      bool ok = mbar_wait(&acc_full[b], aph, err, 5);
-      ok = __all_sync(0xffffffffu, ok);
-      if (!ok) break;
-      tc_fence_after();
-      __syncwarp();
-      const uint32_t tbase = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(b * BN + half * HCOLS);
-      constexpr int NCH = HCOLS / 32;
-      const int ch0 = half * NCH;  // this warp's first 32-column chunk of the tile
-      uint32_t ra[32], rb[32];
-      tmem_ld32(tbase, ra);
-      tmem_wait_ld(ra);
-#pragma unroll 1
-      for (int ch = 0; ch < NCH; ch += 2) {
-        tmem_ld32(tbase + uint32_t((ch + 1) * 32), rb);
+    constexpr int NCH = BN / 32;
+    static_assert(NCH == 4, "the tile loop below handles four 32-column chunks");
+    auto tiles = [&](auto rn_tag) {
+      constexpr bool kRn = decltype(rn_tag)::value;
+      for (int t = 0; t < ntiles; ++t) {
+        const int b = t & 1;
+        const uint32_t aph = (t >> 1) & 1;
+        const int64_t r0 = s_begin + int64_t(t) * BN;
+        if (kRn) reinterpret_cast<float4*>(my_rn)[lane] = __ldg(reinterpret_cast<const float4*>(rn + r0) + lane);
+        if (SHARE) {
+          shared = fminf(shared, bits_key(__ldcg(qb)));
+          thr = fminf(thr, shared);
+        }
+        bool ok = mbar_wait_inl(&acc_full[b], aph, err, 5);
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) return;
+        tc_fence_after();
+        __syncwarp();
+        const uint32_t tbase = tmem + (uint32_t(quarter * 32) << 16) + uint32_t(b) * ACC_COLS + uint32_t(sel * BN);
+        uint32_t ra[32], rb[32];
+        tmem_ld32(tbase, ra);
+        tmem_wait_ld(ra);
+        tmem_ld32(tbase + 32u, rb);
         if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
-        filter(ra, ch0 + ch, r0);
+        process(rn_tag, ra, 0, r0);
         tmem_wait_ld(rb);
-        if (ch + 2 < NCH) tmem_ld32(tbase + uint32_t((ch + 2) * 32), ra);
+        tmem_ld32(tbase + 64u, ra);
         if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
-        filter(rb, ch0 + ch + 1, r0);
-        if (ch + 2 < NCH) tmem_wait_ld(ra);
+        process(rn_tag, rb, 1, r0);
+        tmem_wait_ld(ra);
+        tmem_ld32(tbase + 96u, rb);
+        if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
+        process(rn_tag, ra, 2, r0);
+        tmem_wait_ld(rb);
+        // the last chunk is in registers: hand the accumulator back before
+        // filtering it, so the MMAs of tile t+2 start one chunk earlier
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[b]);
+        if (__any_sync(0xffffffffu, cnt > BUF - 32)) compact();
+        process(rn_tag, rb, 3, r0);
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[b]);
-      __syncwarp();
-    }
+    };
+    // padding references carry |r|^2 = +inf (unfolded) or a huge folded norm
+    if (fold) tiles(std::false_type{});
+    else tiles(std::true_type{});
     compact();
-    // list (split, half) of every query: nsplit * HALVES lists per query
-    int* out = cand + ((int64_t(blockIdx.y) * HALVES + half) * nq_pad + q0 + row) * KC;
+    // list `split` of every query: nsplit lists per query
+    int* out = cand + (int64_t(blockIdx.y) * nq_pad + q0 + row) * KC;
 #pragma unroll
     for (int j = 0; j < KC; ++j) out[j] = top.i[j];
   }
@@ -389,7 +395,7 @@ template <int KC>
 int launch_tc(const CUtensorMap& a, const CUtensorMap& b, const float* rn, int64_t nr, int64_t rps, int nsplit,
               int* cand, int64_t nq_pad, int fold, unsigned* qbound, int* err, cudaStream_t st) {
   const size_t smem = smem_bytes(KC);
-  dim3 grid(unsigned(nq_pad / BM), unsigned(nsplit));
+  dim3 grid(unsigned(nq_pad / BQ), unsigned(nsplit));
   if (nsplit > 1) {
     SG_CUDA(cudaFuncSetAttribute(knn_tc_kernel<KC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     knn_tc_kernel<KC, true><<<grid, THREADS, smem, st>>>(a, b, rn, nr, rps, cand, nq_pad, fold, qbound, err);
@@ -411,19 +417,19 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   int kc = kq + margin;
   if (kc > 64) return sg::fail(SG_ERR_ARG, "sg_knn: k + margin too large (<= 64 candidates per list)");
   kc = kc <= 16 ? 16 : kc <= 32 ? 32 : kc <= 40 ? 40 : kc <= 48 ? 48 : 64;
-  const int64_t nq_pad = sg::ceil_div(nq, BM) * BM;
+  const int64_t nq_pad = sg::ceil_div(nq, BQ) * BQ;
   const int64_t nr_pad = sg::ceil_div(nr, BN) * BN;
   if (nr_pad >= (int64_t(1) << 31) || nq_pad >= (int64_t(1) << 31)) return sg::fail(SG_ERR_ARG, "sg_knn: too many rows");
-  const int qtiles = int(nq_pad / BM);
-  // reference splits per query tile: the heuristic fills ~8 CTAs per SM
+  const int qtiles = int(nq_pad / BQ);
+  // reference splits per query tile: the heuristic fills ~4 CTAs (1024 queries) per SM
   auto splits_for = [&](int want) {
     int ns = std::max(1, want);
-    ns = int(std::min<int64_t>(ns, std::max<int64_t>(1, nr_pad / (BN * 4))));
+    ns = int(std::min<int64_t>(ns, std::max<int64_t>(1, nr_pad / (BN * 8))));
     ns = std::min(ns, 256);
     const int64_t rps_ = sg::ceil_div(sg::ceil_div(nr, ns), BN) * BN;
     return int(sg::ceil_div(nr, rps_));
   };
-  const int ns0 = splits_for(int(std::lround(double(h->sm_count) * 8 / qtiles)));
+  const int ns0 = splits_for(int(std::lround(double(h->sm_count) * 4 / qtiles)));
   auto ilog2 = [](int64_t v) {
     int r = 0;
     while ((int64_t(1) << (r + 1)) <= v) ++r;
@@ -438,7 +444,7 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   const int fold = d <= BK - 3 ? 1 : 0;
   const size_t need = sg::Carver::need(size_t(nr_pad) * BK * 2) + sg::Carver::need(size_t(nr_pad) * 4) +
                       sg::Carver::need(size_t(nq_pad) * BK * 2) +
-                      sg::Carver::need(sizeof(int) * size_t(nsplit) * HALVES * nq_pad * kc) + sg::Carver::need(sizeof(int)) +
+                      sg::Carver::need(sizeof(int) * size_t(nsplit) * nq_pad * kc) + sg::Carver::need(sizeof(int)) +
                       sg::Carver::need(sizeof(unsigned) * size_t(nq_pad));
   int status;
   void* w = sg::ws_get(h, need, &status);
@@ -447,7 +453,7 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   __nv_bfloat16* Rb = cv.take<__nv_bfloat16>(size_t(nr_pad) * BK);
   float* rn = cv.take<float>(nr_pad);
   __nv_bfloat16* Qb = cv.take<__nv_bfloat16>(size_t(nq_pad) * BK);
-  int* cand = cv.take<int>(size_t(nsplit) * HALVES * nq_pad * kc);
+  int* cand = cv.take<int>(size_t(nsplit) * nq_pad * kc);
   int* err = cv.take<int>(1);
   unsigned* qbound = cv.take<unsigned>(size_t(nq_pad));
   SG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
@@ -458,7 +464,7 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   queries_bf16_kernel<<<sg::ceil_div_i(nq_pad, 256), 256, 0, st>>>(queries, nq, d, ld, fold, Qb, nq_pad);
   SG_LAUNCH_CHECK();
   CUtensorMap ta, tb;
-  int rc = make_map(&ta, Qb, nq_pad, BM);
+  int rc = make_map(&ta, Qb, nq_pad, BQ);
   if (rc) return rc;
   rc = make_map(&tb, Rb, nr_pad, BN);
   if (rc) return rc;
@@ -477,7 +483,7 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   if (herr) return sg::fail(SG_ERR_TIMEOUT, "sg_knn: a tensor-core pipeline wait expired (stage %d)", herr);
   sg::ProfScope prof(h, "rerank", st);
   h->last_knn_splits = nsplit;
-  return sg_rerank(queries, refs, d, ld, nq, cand, nsplit * HALVES, kc, nq_pad, kq, k, self_offset, idx_out, dist_out,
+  return sg_rerank(queries, refs, d, ld, nq, cand, nsplit, kc, nq_pad, kq, k, self_offset, idx_out, dist_out,
                    nmiss, st);
   };
   if (tuned) return run(tuned);
