@@ -300,7 +300,7 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
           shared = fminf(shared, bits_key(__ldcg(qb)));
           thr = fminf(thr, shared);
         }
-        bool ok = mbar_wait_inl(&acc_full[b], aph, err, 5);
+        bool ok = mbar_wait(&acc_full[b], aph, err, 5);
         ok = __all_sync(0xffffffffu, ok);
         if (!ok) return;
         tc_fence_after();

@@ -33,9 +33,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
   return ok != 0;
 }
 // Bounded wait: false when the limit expires (the error flag is then raised)
-// or when another thread has already raised it. The inlined form is for
-// threads that hold many live registers (no call boundary to spill across).
-__device__ __forceinline__ bool mbar_wait_inl(uint64_t* b, uint32_t parity, int* err, int code) {
+// or when another thread has already raised it. Always inlined: a call here
+// costs the single-thread TMA and MMA issuers hundreds of nanoseconds per
+// wait, which the tensor pipeline then waits for.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int* err, int code) {
   for (uint32_t it = 0;; ++it) {
     if (mbar_try_wait(b, parity)) return true;
     if ((it & 255u) == 255u) {
@@ -46,9 +47,6 @@ __device__ __forceinline__ bool mbar_wait_inl(uint64_t* b, uint32_t parity, int*
       }
     }
   }
-}
-__device__ __noinline__ inline bool mbar_wait(uint64_t* b, uint32_t parity, int* err, int code) {
-  return mbar_wait_inl(b, parity, err, code);
 }
 __device__ __forceinline__ void fence_barrier_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
