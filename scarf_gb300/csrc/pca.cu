@@ -561,6 +561,10 @@ int solver_handles(sg_handle* h, cudaStream_t st, cusolverDnHandle_t* sol, cubla
   if (!h->blas) {
     cublasHandle_t b;
     SG_BLAS(cublasCreate(&b));
+    // the BF16x9 emulated GEMMs here only see finite operands (a non-finite
+    // block fails the Ritz and residual checks downstream), so the library's
+    // scan-and-patch passes for infinities and NaNs are switched off
+    SG_BLAS(cublasSetEmulationSpecialValuesSupport(b, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE));
     h->blas = b;
   }
   *sol = static_cast<cusolverDnHandle_t>(h->solver);

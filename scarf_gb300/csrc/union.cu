@@ -9,7 +9,7 @@
 // column, puts G's entries before G^T's and keeps input order among
 // duplicates. Buckets are sorted by a warp-level bitonic network in shared
 // memory (<= 256 items) or by a CTA-level bitonic network over a padded scratch
-// region (larger buckets). A walk over each sorted bucket then yields
+// region (larger buckets). A warp-wide walk over each sorted bucket then yields
 // a = sum of G's weights and b = sum of G^T's for every column, and the value
 // in FP64 with the operation order of scipy's sparse add/multiply (no fused
 // multiply-add), so the result is bit-identical to the reference's.
@@ -191,49 +191,61 @@ __device__ __forceinline__ double union_value(bool has_a, bool has_b, double a, 
   return v;
 }
 
+// Warp per row: the bucket is read 32 items at a time (coalesced); the
+// first item of each column group (its head) sums the group's G and G^T
+// weights in bucket order, which is scipy's order, and the kept values are
+// compacted in column order with a ballot.
 template <bool kWrite>
 __global__ void walk_kernel(const unsigned long long* __restrict__ items, const int64_t* __restrict__ bptr, int64_t n,
                             const double* __restrict__ w, double mix, unsigned flags, int* __restrict__ count,
                             const int64_t* __restrict__ optr, int32_t* __restrict__ oind, double* __restrict__ odat,
                             int64_t capacity) {
-  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (r >= n) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t r = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  if (r >= n) return;  // whole warps
   const int64_t a = bptr[r], b = bptr[r + 1];
   const bool upper = flags & SG_UNION_UPPER_ONLY;
-  int cnt = 0;
   int64_t o = kWrite ? optr[r] : 0;
-  int64_t p = a;
-  while (p < b) {
-    const unsigned long long key = items[p];
-    const int64_t col = int64_t(key >> 33);
-    double sa = 0.0, sb = 0.0;
-    bool ha = false, hb = false;
-    while (p < b && int64_t(items[p] >> 33) == col) {
-      const unsigned long long it = items[p];
-      const double wv = w[it & 0xffffffffull];
-      if ((it >> 32) & 1ull) {
-        sb = hb ? __dadd_rn(sb, wv) : wv;
-        hb = true;
-      } else {
-        sa = ha ? __dadd_rn(sa, wv) : wv;
-        ha = true;
-      }
-      ++p;
-    }
-    const double v = union_value(ha, hb, sa, sb, mix);
-    if (v != 0.0 && (!upper || col >= r)) {
-      if (kWrite) {
-        if (o < capacity) {
-          oind[o] = int32_t(col);
-          odat[o] = v;
+  int cnt = 0;
+  for (int64_t base = a; base < b; base += 32) {
+    const int64_t p = base + lane;
+    const bool valid = p < b;
+    const unsigned long long key = valid ? items[p] : 0ull;
+    const long long col = static_cast<long long>(key >> 33);
+    long long prev = __shfl_up_sync(0xffffffffu, col, 1);
+    if (lane == 0) prev = p > a ? static_cast<long long>(items[p - 1] >> 33) : -1;
+    bool keep = false;
+    double v = 0.0;
+    if (valid && col != prev) {
+      double sa = 0.0, sb = 0.0;
+      bool ha = false, hb = false;
+      for (int64_t q = p; q < b; ++q) {
+        const unsigned long long it = q == p ? key : items[q];
+        if (static_cast<long long>(it >> 33) != col) break;
+        const double wv = w[it & 0xffffffffull];
+        if ((it >> 32) & 1ull) {
+          sb = hb ? __dadd_rn(sb, wv) : wv;
+          hb = true;
+        } else {
+          sa = ha ? __dadd_rn(sa, wv) : wv;
+          ha = true;
         }
-        ++o;
-      } else {
-        ++cnt;
+      }
+      v = union_value(ha, hb, sa, sb, mix);
+      keep = v != 0.0 && (!upper || col >= r);
+    }
+    const unsigned ball = __ballot_sync(0xffffffffu, keep);
+    if (kWrite && keep) {
+      const int64_t pos = o + __popc(ball & ((1u << lane) - 1u));
+      if (pos < capacity) {
+        oind[pos] = int32_t(col);
+        odat[pos] = v;
       }
     }
+    o += __popc(ball);
+    cnt += __popc(ball);
   }
-  if (!kWrite) count[r] = cnt;
+  if (!kWrite && lane == 0) count[r] = cnt;
 }
 
 }  // namespace
@@ -295,12 +307,12 @@ extern "C" int sg_fuzzy_union(sg_handle* h, const int64_t* edges, const double* 
   SG_LAUNCH_CHECK();
   sort_big_kernel<<<unsigned(h->sm_count), 1024, 0, st>>>(items, bptr, big, nbig, pad);
   SG_LAUNCH_CHECK();
-  walk_kernel<false><<<sg::ceil_div_i(n, 128), 128, 0, st>>>(items, bptr, n, w, mix, flags, deg, nullptr, nullptr,
+  walk_kernel<false><<<sg::ceil_div_i(n, 8), 256, 0, st>>>(items, bptr, n, w, mix, flags, deg, nullptr, nullptr,
                                                               nullptr, 0);
   SG_LAUNCH_CHECK();
   rc = scan(deg, indptr_out);
   if (rc) return rc;
-  walk_kernel<true><<<sg::ceil_div_i(n, 128), 128, 0, st>>>(items, bptr, n, w, mix, flags, nullptr, indptr_out,
+  walk_kernel<true><<<sg::ceil_div_i(n, 8), 256, 0, st>>>(items, bptr, n, w, mix, flags, nullptr, indptr_out,
                                                              indices_out, data_out, capacity);
   SG_LAUNCH_CHECK();
   unsigned long long hbad = 0;
