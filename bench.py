@@ -141,10 +141,11 @@ def peaks():
 
 # DRAM bytes (read + write) per launch from one ncu capture of the full-size
 # C2 step (dram__bytes_read.sum + dram__bytes_write.sum, one pass; the command
-# and the per-kernel table are in profiles/dram_traffic_make_graph_c2.md)
+# and the per-kernel table are kept under profiles/). "normalize" is the row
+# pass, the column-statistics pass and the partial reductions together.
 DRAM_TRAFFIC = {
-    "c2:normalize": 2_633_393_493, "c2:zsplit": 1_596_762_880, "c2:cov_tc": 1_668_659_200,
-    "c2:project": 819_488_939, "c2:knn_tc": 25_846_699, "c2:rerank": 54_053_632, "c2:smooth": 93_588_053,
+    "c2:normalize": 3_441_743_360, "c2:zsplit": 1_596_976_448, "c2:cov_tc": 1_596_401_152,
+    "c2:project": 819_532_885, "c2:knn_tc": 25_810_858, "c2:rerank": 51_168_460, "c2:smooth": 93_267_626,
 }
 
 
