@@ -501,13 +501,13 @@ def eigensolver_comparison(K, pipeline, ip, ind, dat, G, feat, n, dims, reps=3):
         torch.cuda.synchronize()
         out[f"{method}_ms"] = round(e0.elapsed_time(e1) / reps, 3)
         comps[method] = (c.cpu().numpy(), ev.cpu().numpy())
+        if method == "filter":
+            out["filter_residual"] = K.filter_residual()
 
     def angle(a, b):
         qa, _ = np.linalg.qr(a)
         qb, _ = np.linalg.qr(b)
         return float(np.arccos(np.clip(np.linalg.svd(qa.T @ qb, compute_uv=False), -1, 1)).max())
-        if method == "filter":
-            out["filter_residual"] = K.filter_residual()
     a = comps["fp64"][0]
     for method in ("mixed", "filter"):
         b = comps[method][0]
