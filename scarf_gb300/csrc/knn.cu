@@ -232,6 +232,106 @@ struct KeyList {
   }
 };
 
+// Ascending bitonic sort of the warp's 32 * SLOTS keys, element lane + 32 s in
+// v[s]: partners in other lanes through shuffles, partners in the same lane
+// (distance >= 32) by a local compare-exchange.
+template <int SLOTS>
+__device__ __forceinline__ void warp_bitonic_sort(unsigned long long (&v)[SLOTS], int lane) {
+  constexpr int N = 32 * SLOTS;
+#pragma unroll
+  for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+    for (int j = size >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+#pragma unroll
+        for (int s = 0; s < SLOTS; ++s) {
+          const int t = s ^ (j >> 5);
+          if (t > s) {
+            const bool up = ((lane + 32 * s) & size) == 0;
+            const unsigned long long a = v[s], b = v[t];
+            const bool sw = (a > b) == up;
+            v[s] = sw ? b : a;
+            v[t] = sw ? a : b;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int s = 0; s < SLOTS; ++s) {
+          const int i = lane + 32 * s;
+          const unsigned long long w = __shfl_xor_sync(0xffffffffu, v[s], j);
+          const bool keep_min = ((i & size) == 0) == ((i & j) == 0);
+          const bool lt = v[s] < w;
+          v[s] = (lt == keep_min) ? v[s] : w;
+        }
+      }
+    }
+  }
+}
+
+// Re-rank for at most 32 * SLOTS candidates per query: each lane scores
+// candidates lane + 32 s, the warp sorts the keys, and every lane writes its
+// own output positions; the self rule uses ballots. The same keys in the same
+// total order as the list merge below, so the same output.
+template <int SLOTS>
+__global__ void __launch_bounds__(128)
+rerank_sort_kernel(const float* __restrict__ queries, const float* __restrict__ refs, int d, int ld, int64_t nq,
+                   const int* __restrict__ cand, int nlists, int kc, int64_t nq_pad, int kq, int k,
+                   int64_t self_offset, int64_t* __restrict__ idx_out, float* __restrict__ dist_out,
+                   unsigned long long* __restrict__ nmiss) {
+  __shared__ float qs[4][kMaxD];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t q = int64_t(blockIdx.x) * 4 + warp;
+  if (q >= nq) return;  // whole warps
+  for (int c = lane; c < d; c += 32) qs[warp][c] = queries[q * ld + c];
+  __syncwarp();
+  const int total = nlists * kc;
+  unsigned long long v[SLOTS];
+#pragma unroll
+  for (int s = 0; s < SLOTS; ++s) {
+    v[s] = ~0ull;
+    const int e = lane + 32 * s;
+    if (e >= total) continue;
+    const int ci = cand[(int64_t(e / kc) * nq_pad + q) * kc + e % kc];
+    if (ci < 0) continue;
+    const float* r = refs + int64_t(ci) * ld;
+    float acc = 0.f;
+    for (int c = 0; c < d; ++c) {
+      const float df = qs[warp][c] - __ldg(r + c);
+      acc = fmaf(df, df, acc);
+    }
+    v[s] = (static_cast<unsigned long long>(__float_as_uint(acc)) << 32) | unsigned(ci);
+  }
+  warp_bitonic_sort<SLOTS>(v, lane);
+  // the self rule: drop position 0 when it is self, else the first self among
+  // the first kq (a miss), else the last of them (a miss)
+  int drop = -1;
+  if (self_offset >= 0) {
+    const unsigned self = unsigned(self_offset + q);
+    int first = -1;
+#pragma unroll
+    for (int s = 0; s < SLOTS; ++s) {
+      const bool hit = lane + 32 * s < kq && v[s] != ~0ull && unsigned(v[s] & 0xffffffffu) == self;
+      const unsigned b = __ballot_sync(0xffffffffu, hit);
+      if (first < 0 && b) first = 32 * s + __ffs(int(b)) - 1;
+    }
+    if (first == 0) {
+      drop = 0;
+    } else {
+      if (lane == 0) atomicAdd(nmiss, 1ull);
+      drop = first > 0 ? first : kq - 1;
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < SLOTS; ++s) {
+    const int p = lane + 32 * s;
+    if (p >= kq || p == drop) continue;
+    const int o = drop >= 0 && p > drop ? p - 1 : p;
+    if (o >= k) continue;
+    idx_out[q * k + o] = v[s] == ~0ull ? -1 : int64_t(v[s] & 0xffffffffu);
+    dist_out[q * k + o] = v[s] == ~0ull ? __int_as_float(0x7f800000) : __uint_as_float(unsigned(v[s] >> 32));
+  }
+}
+
 // Stage 2: exact re-rank and self fix. One warp per query; every lane keeps a
 // sorted key list of the candidates it scored, and the warp merges the 32
 // lists by kq rounds of a warp-wide minimum over the list heads.
@@ -327,6 +427,18 @@ int launch_rerank(const float* queries, const float* refs, int d, int ld, int64_
 int sg_rerank(const float* queries, const float* refs, int d, int ld, int64_t nq, const int* cand, int nlists, int kc,
               int64_t nq_pad, int kq, int k, int64_t self_offset, int64_t* idx_out, float* dist_out,
               unsigned long long* nmiss, cudaStream_t st) {
+  const int total = nlists * kc;
+  if (kq <= 64 && total <= 128) {
+    const unsigned grid = unsigned(sg::ceil_div(nq, 4));
+    if (total <= 64)
+      rerank_sort_kernel<2><<<grid, 128, 0, st>>>(queries, refs, d, ld, nq, cand, nlists, kc, nq_pad, kq, k,
+                                                  self_offset, idx_out, dist_out, nmiss);
+    else
+      rerank_sort_kernel<4><<<grid, 128, 0, st>>>(queries, refs, d, ld, nq, cand, nlists, kc, nq_pad, kq, k,
+                                                  self_offset, idx_out, dist_out, nmiss);
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+  }
   if (kq <= 16) return launch_rerank<16>(queries, refs, d, ld, nq, cand, nlists, kc, nq_pad, kq, k, self_offset, idx_out, dist_out, nmiss, st);
   if (kq <= 32) return launch_rerank<32>(queries, refs, d, ld, nq, cand, nlists, kc, nq_pad, kq, k, self_offset, idx_out, dist_out, nmiss, st);
   return launch_rerank<64>(queries, refs, d, ld, nq, cand, nlists, kc, nq_pad, kq, k, self_offset, idx_out, dist_out, nmiss, st);
