@@ -262,6 +262,32 @@ def test_pca_basis_and_projection(K, counts):
     assert torch.all(scores[:, dims:] == 0)
 
 
+def test_projection_gemm_path(K):
+    """From 4,096 rows the projection is one tensor-core GEMM over the
+    uncentred rows with the centring folded into a per-column shift; it agrees
+    with the oracle's reducer on the same basis, pads with zeros and writes
+    the optional BF16 copy."""
+    indptr, indices, data, G, _ = small_counts(n_cells=6000, seed=3)
+    feat = top_var_genes(indptr, indices, data, G, 300)
+    counts = (indptr, indices, data, G, feat)
+    x, cs, cq, _ = _normalize(K, counts)
+    mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
+    xw, omu, osg, z = _zscaled(counts)
+    h = z.shape[1]
+    dims = 30
+    cov, zsum = K.covariance(x, mu32, sg32, n_cols=h)
+    comps, _, _, l32 = K.pca_basis(cov, zsum, x.shape[0], dims + 1, n_load=dims, ld_l=dims)
+    assert x.shape[0] >= 4096
+    scores, sb = K.project(x, mu32, sg32, l32, dims, n_cols=h, ld_s=32, bf16_ld=40)
+    torch.cuda.synchronize()
+    want = oracle.reducer(xw, omu, osg, comps.cpu().numpy()[:, :dims])
+    got = scores[:, :dims].cpu().numpy()
+    assert np.abs(got - want).max() <= 1e-4 * max(1.0, np.abs(want).max())
+    assert torch.all(scores[:, dims:] == 0)
+    assert torch.all(sb[:, dims:].float() == 0)
+    assert torch.equal(sb[:, :dims], scores[:, :dims].to(torch.bfloat16))
+
+
 def _self_knn(K, pts, k, **kw):
     t = cu(np.pad(pts, ((0, 0), (0, (-pts.shape[1]) % 4))))
     idx, dist, nm = K.knn(t, t, pts.shape[1], k, self_offset=0, **kw)
