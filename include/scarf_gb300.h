@@ -228,6 +228,21 @@ int sg_fuzzy_union(sg_handle* h, const int64_t* edges, const double* w, int64_t 
                    int32_t k, int32_t use_k, double mix, uint32_t flags, int64_t* indptr_out,
                    int32_t* indices_out, double* data_out, int64_t capacity, void* stream);
 
+/* f1 -- the MiniBatchKMeans step of make_graph (scarf/ann.py:328-346):
+ * MiniBatchKMeans(n_clusters=k, random_state=seed, batch_size=block_rows)
+ * partial_fit over the row blocks of x[n x d] (row stride ld, a multiple of 4)
+ * in order, then predict for every row. The first block initialises the
+ * centres (its rows in order when it has exactly k rows, else greedy
+ * k-means++); each block then moves the centres it is nearest to with
+ * scikit-learn's count-weighted update (FP64) and reassigns centres below
+ * 0.01 x the largest weight every 10 k rows or while one has no weight.
+ * Random draws come from a counter hash of `seed`, not numpy's generator.
+ * centers_out[k*d] float64 (row-major), labels_out[n] int32. 1 <= k <= 2048,
+ * k <= block_rows <= 4096, d <= 64. */
+int sg_kmeans_minibatch(sg_handle* h, const float* x, int64_t n, int32_t d, int32_t ld, int32_t k,
+                        int32_t block_rows, uint64_t seed, double* centers_out, int32_t* labels_out,
+                        void* stream);
+
 #ifdef __cplusplus
 }
 #endif

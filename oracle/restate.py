@@ -12,7 +12,12 @@ it is restated from its published algorithm:
 * scikit-learn 1.6.1 ``IncrementalPCA.partial_fit`` and ``svd_flip``
   (``requirements.txt:16``);
 * hnswlib 0.8.0 (``requirements.txt:3``) is *not* restated: the oracle is an
-  exact FP64 kNN, which is what the GPU path is measured against.
+  exact FP64 kNN, which is what the GPU path is measured against;
+* scikit-learn 1.6.1 ``MiniBatchKMeans.partial_fit`` / ``predict``
+  (``sklearn/cluster/_kmeans.py``: ``_mini_batch_step``, ``_random_reassign``,
+  ``_kmeans_plusplus``; ``_k_means_minibatch.pyx``: ``_minibatch_update_dense``)
+  with its random draws taken from the counter hash of the GPU kernel instead
+  of numpy's generator (``kmeans_minibatch``).
 """
 
 from __future__ import annotations
@@ -38,6 +43,8 @@ __all__ = [
     "smooth_knn_dist",
     "compute_membership_strengths",
     "smoothen_dists",
+    "kmeans_hash",
+    "kmeans_minibatch",
     "store_to_sparse",
     "symmetrize",
     "fuzzy_simplicial_set",
@@ -582,3 +589,101 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int, k: int,
     edges, weights = smoothen_dists(ki, kd, lc, bw, batch_size)
     return dict(x=x, scalar=scalar, mu=mu, sigma=sigma, loadings=loadings, scores=scores,
                 indices=ki, distances=kd, recall=recall, edges=edges, weights=weights)
+
+
+# ---- f1: MiniBatchKMeans of make_graph (scarf/ann.py:328-346) ---------------
+
+_M64 = (1 << 64) - 1
+
+
+def kmeans_hash(seed: int, stream: int, i) -> np.ndarray:
+    """The kernel's counter hash (SplitMix64's finaliser) of seed, stream and
+    index, as uint64 (wrapping arithmetic)."""
+    with np.errstate(over="ignore"):
+        i = np.asarray(i, dtype=np.uint64)
+        z = np.uint64(seed & _M64) + (np.uint64((stream << 32) & _M64) + i) * np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def _kmeans_unit(seed: int, stream: int, i) -> np.ndarray:
+    return (kmeans_hash(seed, stream, i) >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def _sq_dists(x: np.ndarray, c: np.ndarray) -> np.ndarray:
+    x64 = x.astype(np.float64)
+    c64 = c.astype(np.float64)
+    return ((x64[:, None, :] - c64[None, :, :]) ** 2).sum(-1)
+
+
+def _kmeans_plusplus(x: np.ndarray, k: int, seed: int) -> np.ndarray:
+    """Greedy k-means++ (sklearn _kmeans_plusplus, 2 + ln k local trials),
+    draws from the counter hash: the first centre uniformly, round c's
+    candidates at cumsum(D2) >= u * total."""
+    rows = x.shape[0]
+    trials = 2 + int(np.log(k))
+    chosen = int(_kmeans_unit(seed, 1, 0) * rows) % rows
+    centers = np.empty((k, x.shape[1]), dtype=np.float64)
+    d2 = None
+    for c in range(k):
+        centers[c] = x[chosen]
+        t = _sq_dists(x, x[chosen:chosen + 1])[:, 0]
+        d2 = t if d2 is None else np.minimum(d2, t)
+        if c + 1 == k:
+            break
+        csum = np.cumsum(d2)
+        r = _kmeans_unit(seed, 2 + c, np.arange(trials)) * csum[-1]
+        cid = np.minimum(np.searchsorted(csum, r, side="left"), rows - 1)
+        pots = [np.minimum(d2, _sq_dists(x, x[j:j + 1])[:, 0]).sum() for j in cid]
+        chosen = int(cid[int(np.argmin(pots))])
+    return centers
+
+
+def kmeans_minibatch(x: np.ndarray, k: int, block_rows: int, seed: int):
+    """partial_fit over the row blocks of x in order, then predict
+    (scarf/ann.py:328-346 with sklearn's MiniBatchKMeans semantics, see the
+    module docstring). Returns (centres f64 k x d, labels int64)."""
+    x = np.asarray(x, dtype=np.float32)
+    n = x.shape[0]
+    first = min(n, block_rows)
+    if first < k:
+        raise ValueError("the first block has fewer rows than k")
+    centers = x[:k].astype(np.float64) if first == k else _kmeans_plusplus(x[:first], k, seed)
+    w = np.zeros(k)
+    since = 0
+    for step, r0 in enumerate(range(0, n, block_rows)):
+        xb = x[r0:r0 + block_rows]
+        rows = xb.shape[0]
+        # _random_reassign (checked before the update, counted in first-block sizes)
+        since += first
+        reassign = bool((w == 0).any()) or since >= 10 * k
+        if reassign:
+            since = 0
+        lab = np.argmin(_sq_dists(xb, centers.astype(np.float32)), axis=1)
+        for c in np.unique(lab):
+            members = np.nonzero(lab == c)[0]
+            v = centers[c] * w[c]
+            for m in members:
+                v = v + xb[m].astype(np.float64)
+            w_new = w[c] + len(members)
+            centers[c] = v * (1.0 / w_new)
+            w[c] = w_new
+        if not reassign:
+            continue
+        flagged = np.nonzero(w < 0.01 * w.max())[0]
+        cap = int(0.5 * rows)
+        if len(flagged) > cap:
+            flagged = np.sort(flagged[np.argsort(w[flagged], kind="stable")][:cap])
+        m = len(flagged)
+        if m == 0:
+            continue
+        keys = (kmeans_hash(seed, 0x80000000 + step, np.arange(rows)) & np.uint64(~0xFFF & _M64)) | \
+            np.arange(rows, dtype=np.uint64)
+        pick = np.argsort(keys, kind="stable")[:m]
+        rest = np.ones(k, dtype=bool)
+        rest[flagged] = False
+        centers[flagged] = xb[pick].astype(np.float64)
+        w[flagged] = w[rest].min()
+    labels = np.argmin(_sq_dists(x, centers.astype(np.float32)), axis=1).astype(np.int64)
+    return centers, labels

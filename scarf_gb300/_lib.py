@@ -31,6 +31,7 @@ vp = C.c_void_p
 i32 = C.c_int32
 i64 = C.c_int64
 u32 = C.c_uint32
+u64 = C.c_uint64
 f32 = C.c_float
 f64 = C.c_double
 sz = C.c_size_t
@@ -61,6 +62,7 @@ SIGNATURES = {
     "sg_smooth": (C.c_int, [vp, vp, vp, i64, i32, f64, f64, i64, vp, vp, vp]),
     "sg_smooth_noalloc": (C.c_int, [vp, vp, i64, i32, f64, f64, i64, vp, vp, vp]),
     "sg_fuzzy_union": (C.c_int, [vp, vp, vp, i64, i64, i32, i32, f64, u32, vp, vp, vp, i64, vp]),
+    "sg_kmeans_minibatch": (C.c_int, [vp, vp, i64, i32, i32, i32, i32, u64, vp, vp, vp]),
 }
 
 _lock = threading.Lock()

@@ -172,6 +172,16 @@ class _PcaInfo:
         self.n_samples_seen_ = n_samples
 
 
+class KMeansResult:
+    """What make_graph reads from the fitted MiniBatchKMeans: ``cluster_centers_`` (k x dims, float64) and
+    ``labels_`` (the predicted label of every cell)."""
+
+    def __init__(self, centers: np.ndarray, labels: np.ndarray):
+        self.cluster_centers_ = centers
+        self.labels_ = labels
+        self.n_clusters = centers.shape[0]
+
+
 class AnnStream:
     """scarf/ann.py:55-205 on the GPU (see the module docstring)."""
 
@@ -246,10 +256,21 @@ class AnnStream:
             self.annIdx = ann_idx
             self.annIdx.set_ef(self.annEf)
             self.annIdx.set_num_threads(self.annThreads)
-        self.kmeans = None
-        if do_kmeans_fit:
-            log.info("k-means seeding (MiniBatchKMeans, used for initial UMAP/tSNE embeddings) is not part of "
-                     "this build; cluster labels stay -1")
+        self.kmeans = self._fit_kmeans(do_kmeans_fit)
+
+    def _fit_kmeans(self, do_kmeans_fit: bool):
+        """scarf/ann.py:328-346 on the GPU: MiniBatchKMeans(n_clusters, random_state, batch_size) partial_fit
+        over the blocks of the reduced data, then predict (sg_kmeans_minibatch). Sets ``clusterLabels``."""
+        if do_kmeans_fit is False:
+            return None
+        try:
+            centers, labels = K.kmeans(self.scores, self.dims, int(self.nClusters), int(self.batchSize),
+                                       int(self.randState))
+        except ValueError as e:  # sizes outside the kernel's limits: the seeding labels stay -1
+            log.warning(f"k-means seeding skipped: {e}")
+            return None
+        self.clusterLabels = labels.cpu().numpy().astype(np.int64)
+        return KMeansResult(centers.cpu().numpy(), self.clusterLabels)
 
     def _handle_batch_size(self):
         if self.dims is not None and self.dims > self.data.shape[0]:

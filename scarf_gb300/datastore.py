@@ -292,6 +292,13 @@ class DataStore:
         if reduction_loc not in zw or "reduction" not in zw[reduction_loc]:
             g = zw.create_group(reduction_loc, overwrite=reduction_loc not in zw)
             create_zarr_dataset(g, "reduction", data.chunksize, "f8", ann_obj.loadings.shape)[:, :] = ann_obj.loadings
+        if ann_obj.kmeans is not None:
+            # graph_datastore.py:958-975: centres and labels of the seeding k-means
+            g = zw.create_group(kmeans_loc, overwrite=True)
+            cc = ann_obj.kmeans.cluster_centers_
+            create_zarr_dataset(g, "cluster_centers", (1000, 1000), "f8", cc.shape)[:, :] = cc
+            create_zarr_dataset(g, "cluster_labels", (100000,), "f8", ann_obj.clusterLabels.shape)[:] = \
+                ann_obj.clusterLabels
         if ann_loc not in zw:
             zw.create_group(ann_loc)
         if ann_index_saver is not None:

@@ -259,6 +259,22 @@ def smooth(idx: torch.Tensor, dist: torch.Tensor, local_connectivity: float, ban
     return edges, w
 
 
+def kmeans(x: torch.Tensor, d: int, n_clusters: int, block_rows: int, seed: int):
+    """f1: MiniBatchKMeans of make_graph (see sg_kmeans_minibatch): partial_fit
+    over the row blocks of ``x`` (n x ld float32, rows of ``d`` values) in
+    order, then predict. Returns ``(centres float64 (k, d), labels int32 (n,))``."""
+    _need(x, "x", torch.float32, 2)
+    if x.stride(0) % 4:
+        raise ValueError("x's row stride must be a multiple of 4 floats")
+    dev = x.device
+    centers = torch.empty((n_clusters, d), dtype=torch.float64, device=dev)
+    labels = torch.empty(x.shape[0], dtype=torch.int32, device=dev)
+    L.check(L.load().sg_kmeans_minibatch(handle(dev.index).ptr, _p(x), x.shape[0], d, x.stride(0), n_clusters,
+                                         block_rows, C.c_uint64(int(seed) & ((1 << 64) - 1)), _p(centers),
+                                         _p(labels), _stream(dev)))
+    return centers, labels
+
+
 def fuzzy_union(edges: torch.Tensor, w: torch.Tensor, n: int, k: int, use_k: Optional[int] = None,
                 mix: float = 1.0, upper_only: bool = False) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
     """a9: CSR (indptr int64, indices int32, data float64) of the fuzzy union."""

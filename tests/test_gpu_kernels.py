@@ -450,3 +450,37 @@ def test_fuzzy_union_use_k_upper_and_hubs(K):
         assert np.array_equal(ip.cpu().numpy(), want.indptr)
         assert np.array_equal(ind.cpu().numpy(), want.indices)
         assert np.array_equal(dat.cpu().numpy(), want.data)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,d,k,block,clusters", [(1500, 10, 500, 500, 12), (20000, 16, 100, 1000, 30),
+                                                  (5000, 30, 64, 777, 8)])
+def test_kmeans_minibatch_matches_oracle(K, n, d, k, block, clusters):
+    """sg_kmeans_minibatch against the oracle's restatement (same draws from
+    the counter hash): rows-in-order init (k = block) and k-means++ init with
+    reassignment and a ragged last block. FP32 assignment distances on the GPU
+    against FP64 in the oracle can split a near-tie, so labels must agree on
+    99.9% of rows and the centres' inertia to 1e-6."""
+    x = clustered_points(n, d, n_clusters=clusters, seed=n + d)
+    ld = -(-d // 4) * 4
+    t = torch.zeros((n, ld), dtype=torch.float32, device="cuda")
+    t[:, :d] = cu(x)
+    centers, labels = K.kmeans(t, d, k, block, 4466)
+    torch.cuda.synchronize()
+    c_o, l_o = oracle.kmeans_minibatch(x, k, block, 4466)
+    got_c = centers.cpu().numpy()
+    got_l = labels.cpu().numpy().astype(np.int64)
+    assert got_c.shape == (k, d) and got_l.shape == (n,)
+    assert np.mean(got_l == l_o) >= 0.999
+    inertia = lambda c, l: float(((x.astype(np.float64) - c[l]) ** 2).sum())
+    assert abs(inertia(got_c, got_l) / inertia(c_o, l_o) - 1.0) < 1e-6
+    assert np.abs(got_c - c_o).max() <= 1e-5 * max(1.0, np.abs(c_o).max())
+
+
+@pytest.mark.gpu
+def test_kmeans_minibatch_rejects_bad_sizes(K):
+    t = torch.zeros((100, 8), dtype=torch.float32, device="cuda")
+    with pytest.raises(ValueError):
+        K.kmeans(t, 8, 200, 100, 1)   # first block smaller than k
+    with pytest.raises(ValueError):
+        K.kmeans(t, 8, 10, 5000, 1)   # block above the kernel's limit

@@ -144,3 +144,58 @@ def test_exact_knn_tie_order():
     assert i[0].tolist() == [0, 1, 2, 3]
     assert i[1].tolist() == [1, 2, 0, 3]
     assert i[2].tolist() == [1, 2, 0, 3]
+
+
+def _sklearn_minibatch(x, k, block, seed):
+    cluster = pytest.importorskip("sklearn.cluster")
+    import warnings
+    km = cluster.MiniBatchKMeans(n_clusters=k, random_state=seed, batch_size=block, n_init=3)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for r0 in range(0, len(x), block):
+            km.partial_fit(x[r0:r0 + block].astype(np.float64))
+    return km.cluster_centers_, km.predict(x.astype(np.float64))
+
+
+def test_kmeans_minibatch_matches_sklearn_when_it_draws_nothing():
+    """k = block rows: k-means++ picks every row of the first block (in a
+    random order) and no centre is ever light enough to be reassigned, so
+    scikit-learn's MiniBatchKMeans is deterministic up to the order of its
+    centres, and the restatement reproduces it exactly."""
+    from helpers import clustered_points
+    x = clustered_points(1500, 10, n_clusters=12, seed=5)
+    c_o, l_o = oracle.kmeans_minibatch(x, 500, 500, 4466)
+    c_s, l_s = _sklearn_minibatch(x, 500, 500, 4466)
+    d = ((c_o[:, None, :] - c_s[None, :, :]) ** 2).sum(-1)
+    perm = d.argmin(1)
+    assert len(np.unique(perm)) == 500
+    assert np.sqrt(d.min(1)).max() == 0.0
+    assert np.array_equal(perm[l_o], l_s)
+
+
+def test_kmeans_minibatch_quality_with_kmeans_plusplus_and_reassignment():
+    """k < block rows (k-means++ on the first block) over 20 blocks, where the
+    periodic reassignment check runs: the draws differ from numpy's, so the
+    result is compared by inertia."""
+    from helpers import clustered_points
+    x = clustered_points(20000, 16, n_clusters=30, seed=7)
+    c_o, l_o = oracle.kmeans_minibatch(x, 100, 1000, 4466)
+    c_s, l_s = _sklearn_minibatch(x, 100, 1000, 4466)
+    inertia = lambda c, l: float(((x.astype(np.float64) - c[l]) ** 2).sum())
+    assert abs(inertia(c_o, l_o) / inertia(c_s, l_s) - 1.0) < 0.05
+    # every label is the nearest centre
+    d = ((x[:, None, :].astype(np.float64) - c_o[None].astype(np.float32).astype(np.float64)) ** 2).sum(-1)
+    assert np.array_equal(d.argmin(1), l_o)
+
+
+def test_kmeans_hash_is_the_splitmix64_finaliser():
+    """The counter hash both the kernel and the restatement draw from:
+    SplitMix64's output function of seed + (stream * 2^32 + i) * golden."""
+    def ref(seed, stream, i):
+        m = (1 << 64) - 1
+        z = (seed + ((stream << 32) + i) * 0x9E3779B97F4A7C15) & m
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+        return z ^ (z >> 31)
+    for seed, stream, i in ((4466, 1, 0), (0, 2, 7), ((1 << 64) - 5, 0x80000000 + 3, 4095)):
+        assert int(oracle.kmeans_hash(seed, stream, i)) == ref(seed, stream, i)
