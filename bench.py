@@ -401,6 +401,20 @@ def run_gb300(args, cfg):
     K.profile(False)
     if c_u:
         prof_ms["union"] = (t_u / c_u, 0.0)
+    # the k-means seeding step of make_graph (MiniBatchKMeans, 1,000 centres,
+    # blocks of the batch size), reported beside the step as the reference
+    # does not count it in make_graph's graph time
+    n_cent = min(1000, BATCH)
+    K.kmeans(res.scores, dims, n_cent, BATCH, 4466)
+    torch.cuda.synchronize()
+    st_k = torch.cuda.current_stream()
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record(st_k)
+    K.kmeans(res.scores, dims, n_cent, BATCH, 4466)
+    k1.record(st_k)
+    torch.cuda.synchronize()
+    kmeans_info = {"ms": round(k0.elapsed_time(k1), 3), "n_clusters": n_cent, "block_rows": BATCH,
+                   "note": "partial_fit per block of the scores, then predict; not part of ms_per_step"}
     eig = eigensolver_comparison(K, pipeline, ip_d, ind_d, dat_d, G, feat, n, dims)
     pk = peaks()
     work = kernel_work(cfg, csr.nnz)
@@ -463,6 +477,7 @@ def run_gb300(args, cfg):
         "kernels": kernels,
         "eigh_parts": eig_parts,
         "eigensolver": eig,
+        "kmeans": kmeans_info,
         "e2e": {"value": round(cells / (e2e_ms * 1e-3), 1), "unit": "cells/s", "ms_per_step": round(e2e_ms, 3),
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": roof,

@@ -685,5 +685,7 @@ def kmeans_minibatch(x: np.ndarray, k: int, block_rows: int, seed: int):
         rest[flagged] = False
         centers[flagged] = xb[pick].astype(np.float64)
         w[flagged] = w[rest].min()
-    labels = np.argmin(_sq_dists(x, centers.astype(np.float32)), axis=1).astype(np.int64)
+    c32 = centers.astype(np.float32)
+    labels = np.concatenate([np.argmin(_sq_dists(x[a:a + 2048], c32), axis=1)
+                             for a in range(0, n, 2048)]).astype(np.int64)
     return centers, labels
