@@ -243,6 +243,24 @@ int sg_kmeans_minibatch(sg_handle* h, const float* x, int64_t n, int32_t d, int3
                         int32_t block_rows, uint64_t seed, double* centers_out, int32_t* labels_out,
                         void* stream);
 
+/* f4 -- calc_snn (scarf/knn_utils.py:195-211): snn_out[i*k + j] =
+ * |set(indices[i]) & set(indices[m])| / (k - 1) with m = indices[i*k + j]
+ * (int64, row-major n x k; a negative m counts from the end, an m outside
+ * [-n, n) scores 0). 2 <= k <= 64. */
+int sg_calc_snn(sg_handle* h, const int64_t* indices, int64_t n, int32_t k, double* snn_out, void* stream);
+
+/* f4 -- merge_graphs + weight_sort_indices (scarf/knn_utils.py:214-274) of
+ * n_graphs kNN graphs of n rows and k neighbours each, given as host arrays
+ * of device pointers: indices[g] (n x k int64), w[g] (n x k float64) and
+ * snn[g] (n x k float64, from sg_calc_snn). Per row the candidates are ordered
+ * by w + snn, largest first (ties: the later candidate first), the first
+ * occurrence of each neighbour is kept, and the first k go to out_indices /
+ * out_w (n x k; -1 / 0 pad a row with fewer than k distinct neighbours).
+ * 1 <= n_graphs <= 8, n_graphs * k <= 128. */
+int sg_merge_graphs(sg_handle* h, int32_t n_graphs, const int64_t* const* indices, const double* const* w,
+                    const double* const* snn, int64_t n, int32_t k, int64_t* out_indices, double* out_w,
+                    void* stream);
+
 #ifdef __cplusplus
 }
 #endif

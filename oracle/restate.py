@@ -45,6 +45,9 @@ __all__ = [
     "smoothen_dists",
     "kmeans_hash",
     "kmeans_minibatch",
+    "calc_snn",
+    "weight_sort_indices",
+    "merge_graphs",
     "store_to_sparse",
     "symmetrize",
     "fuzzy_simplicial_set",
@@ -689,3 +692,48 @@ def kmeans_minibatch(x: np.ndarray, k: int, block_rows: int, seed: int):
     labels = np.concatenate([np.argmin(_sq_dists(x[a:a + 2048], c32), axis=1)
                              for a in range(0, n, 2048)]).astype(np.int64)
     return centers, labels
+
+
+# ---- f4: shared neighbours and graph merging (scarf/knn_utils.py:195-274) ---
+
+
+def calc_snn(indices: np.ndarray) -> np.ndarray:
+    """scarf/knn_utils.py:195-211: |set(row i) & set(row of its j-th
+    neighbour)| / (k - 1) for every edge."""
+    n, k = indices.shape
+    sets = [set(r.tolist()) for r in indices]
+    snn = np.zeros((n, k))
+    for i in range(n):
+        for j in range(k):
+            snn[i, j] = len(sets[i] & sets[int(indices[i, j])])
+    return snn / (k - 1)
+
+
+def weight_sort_indices(i: np.ndarray, w: np.ndarray, wn: np.ndarray, n: int):
+    """scarf/knn_utils.py:214-233: order by wn, largest first, keep the first
+    occurrence of each index, the first n. The reference reverses numpy's
+    default (unstable) argsort, so tied wn values have no fixed order there;
+    here ties put the later candidate first (a stable argsort, reversed)."""
+    idx = np.argsort(wn, kind="stable")[::-1]
+    i = i[idx]
+    w = w[idx]
+    _, first = np.unique(i, return_index=True)
+    first = sorted(first)
+    return i[first][:n], w[first][:n]
+
+
+def merge_graphs(csr_mats):
+    """scarf/knn_utils.py:236-274 (returns a scipy COO matrix)."""
+    nk = int(csr_mats[0].indptr[1] - csr_mats[0].indptr[0])
+    n = csr_mats[0].shape[0]
+    snns = [calc_snn(m.indices.reshape(n, nk)) for m in csr_mats]
+    col, data = [], []
+    for r in range(n):
+        mi = np.hstack([m.indices[m.indptr[r]:m.indptr[r + 1]] for m in csr_mats])
+        mw = np.hstack([m.data[m.indptr[r]:m.indptr[r + 1]] for m in csr_mats])
+        mwn = np.hstack([m.data[m.indptr[r]:m.indptr[r + 1]] + snns[g][r] for g, m in enumerate(csr_mats)])
+        a, b = weight_sort_indices(mi, mw, mwn, nk)
+        col.extend(a)
+        data.extend(b)
+    row = np.repeat(np.arange(n), nk)
+    return sp.coo_matrix((data, (row, col)), shape=csr_mats[0].shape)

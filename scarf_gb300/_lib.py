@@ -63,6 +63,8 @@ SIGNATURES = {
     "sg_smooth_noalloc": (C.c_int, [vp, vp, i64, i32, f64, f64, i64, vp, vp, vp]),
     "sg_fuzzy_union": (C.c_int, [vp, vp, vp, i64, i64, i32, i32, f64, u32, vp, vp, vp, i64, vp]),
     "sg_kmeans_minibatch": (C.c_int, [vp, vp, i64, i32, i32, i32, i32, u64, vp, vp, vp]),
+    "sg_calc_snn": (C.c_int, [vp, vp, i64, i32, vp, vp]),
+    "sg_merge_graphs": (C.c_int, [vp, i32, vp, vp, vp, i64, i32, vp, vp, vp]),
 }
 
 _lock = threading.Lock()

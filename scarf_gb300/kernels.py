@@ -275,6 +275,39 @@ def kmeans(x: torch.Tensor, d: int, n_clusters: int, block_rows: int, seed: int)
     return centers, labels
 
 
+def calc_snn(indices: torch.Tensor) -> torch.Tensor:
+    """f4: shared-neighbour fractions of a kNN graph (see sg_calc_snn); ``indices`` n x k int64."""
+    _need(indices, "indices", torch.int64, 2)
+    n, k = indices.shape
+    out = torch.empty((n, k), dtype=torch.float64, device=indices.device)
+    L.check(L.load().sg_calc_snn(handle(indices.device.index).ptr, _p(indices), n, k, _p(out),
+                                 _stream(indices.device)))
+    return out
+
+
+def merge_graphs(indices, weights, snns):
+    """f4: merge of kNN graphs (see sg_merge_graphs). Each argument is a list
+    of n x k CUDA tensors (int64, float64, float64), one per graph. Returns
+    ``(indices int64 (n, k), weights float64 (n, k))``."""
+    if not (len(indices) == len(weights) == len(snns)) or not indices:
+        raise ValueError("one indices, weights and snn tensor per graph")
+    n, k = indices[0].shape
+    dev = indices[0].device
+    for a, b, c in zip(indices, weights, snns):
+        _need(a, "indices", torch.int64, 2)
+        _need(b, "weights", torch.float64, 2)
+        _need(c, "snn", torch.float64, 2)
+        if a.shape != (n, k) or b.shape != (n, k) or c.shape != (n, k):
+            raise ValueError("all graphs must have the same shape")
+    g = len(indices)
+    arr = lambda ts: (C.c_void_p * g)(*[t.data_ptr() for t in ts])
+    out_i = torch.empty((n, k), dtype=torch.int64, device=dev)
+    out_w = torch.empty((n, k), dtype=torch.float64, device=dev)
+    L.check(L.load().sg_merge_graphs(handle(dev.index).ptr, g, arr(indices), arr(weights), arr(snns), n, k,
+                                     _p(out_i), _p(out_w), _stream(dev)))
+    return out_i, out_w
+
+
 def fuzzy_union(edges: torch.Tensor, w: torch.Tensor, n: int, k: int, use_k: Optional[int] = None,
                 mix: float = 1.0, upper_only: bool = False) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
     """a9: CSR (indptr int64, indices int32, data float64) of the fuzzy union."""

@@ -63,3 +63,32 @@ def make_knn_graph(ann_obj, knn_store, graph_store, chunk_size: int, lc: float =
     ind, dist = ann_obj._last_knn
     smoothen_dists(graph_store, ind, dist, lc, bw, chunk_size)
     return recall
+
+
+def calc_snn(indices: np.ndarray) -> np.ndarray:
+    """scarf/knn_utils.py:195-211 on the GPU: for every edge (i, j) the number of
+    neighbours row i shares with its j-th neighbour, over k - 1."""
+    t = torch.as_tensor(np.ascontiguousarray(indices), dtype=torch.int64).cuda()
+    return K.calc_snn(t).cpu().numpy()
+
+
+def merge_graphs(csr_mats):
+    """scarf/knn_utils.py:236-274 on the GPU: merge kNN graphs of the same shape
+    and size so that every row keeps k edges, chosen by weight + shared
+    neighbours. Returns a ``scipy.sparse.coo_matrix``."""
+    from scipy.sparse import coo_matrix
+    if len(set(x.shape for x in csr_mats)) != 1:
+        raise ValueError("ERROR: All graphs do not have the same shape.")
+    if len(set(x.size for x in csr_mats)) != 1:
+        raise ValueError("ERROR: All graphs do not have the same number of edges")
+    n = csr_mats[0].shape[0]
+    nk = int(csr_mats[0].indptr[1] - csr_mats[0].indptr[0])
+    idx, w, snn = [], [], []
+    for mat in csr_mats:
+        i = torch.as_tensor(mat.indices.reshape(n, nk).astype(np.int64)).cuda()
+        idx.append(i)
+        w.append(torch.as_tensor(mat.data.reshape(n, nk).astype(np.float64)).cuda())
+        snn.append(K.calc_snn(i))
+    oi, ow = K.merge_graphs(idx, w, snn)
+    row = np.repeat(np.arange(n), nk)
+    return coo_matrix((ow.cpu().numpy().ravel(), (row, oi.cpu().numpy().ravel())), shape=csr_mats[0].shape)

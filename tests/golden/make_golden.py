@@ -18,7 +18,8 @@ Two kinds of fixtures are written:
   out of its module with ``ast`` and executed in a namespace holding numpy,
   scipy and scikit-learn (and, for ``smoothen_dists``, the oracle's
   restatement of the two umap-learn functions it calls, so that the chunk
-  loop and the ``global_min`` fix of the reference are what is pinned).
+  loop and the ``global_min`` fix of the reference are what is pinned;
+  ``calc_snn`` runs without its numba ``jit`` decorator).
 
 The fixtures are committed; this script is the recipe that made them.
 """
@@ -232,6 +233,26 @@ def main(ref_root: str):
     out.update(pca_x=zp, pca_mu=mu_p, pca_sigma=sd_p, pca_use=use, pca_dims=np.int64(6),
                pca_batch=np.int64(150), pca_loadings=fake.loadings,
                pca_evr=fake._pca.explained_variance_ratio_)
+
+    # --- calc_snn, weight_sort_indices, merge_graphs (knn_utils.py:195-274) --
+    ns = {"np": np, "jit": lambda **kw: (lambda f: f), "tqdmbar": lambda x, **kw: x,
+          "csr_matrix": sp.csr_matrix, "coo_matrix": sp.coo_matrix, "List": list, "Tuple": tuple}
+    snn_f = lift(ref / "knn_utils.py", "calc_snn", ns)
+    lift(ref / "knn_utils.py", "weight_sort_indices", ns)
+    merge_f = lift(ref / "knn_utils.py", "merge_graphs", ns)
+    nm, km = 240, 7
+    mats = []
+    for gidx in range(2):
+        mi = np.stack([rng.choice(nm, km, replace=False) for _ in range(nm)])
+        if gidx == 1:
+            mi[:, :3] = mats[0].indices.reshape(nm, km)[:, :3]   # neighbours shared by both graphs
+        mw = rng.random(nm * km).astype(np.float32).astype(np.float64)
+        mats.append(sp.csr_matrix((mw, mi.ravel(), np.arange(0, nm * km + 1, km)), shape=(nm, nm)))
+        out[f"merge_g{gidx}_indices"] = mi
+        out[f"merge_g{gidx}_data"] = mw
+        out[f"merge_g{gidx}_snn"] = snn_f(mi)
+    mg = merge_f(mats)
+    out.update(merge_n=np.int64(nm), merge_k=np.int64(km), merge_row=mg.row, merge_col=mg.col, merge_data=mg.data)
 
     np.savez_compressed(HERE / "ref_functions.npz", **out)
     print("wrote", sorted(out))

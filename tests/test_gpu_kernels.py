@@ -484,3 +484,61 @@ def test_kmeans_minibatch_rejects_bad_sizes(K):
         K.kmeans(t, 8, 200, 100, 1)   # first block smaller than k
     with pytest.raises(ValueError):
         K.kmeans(t, 8, 10, 5000, 1)   # block above the kernel's limit
+
+
+@pytest.mark.gpu
+def test_calc_snn_and_merge_graphs_golden(K, golden_dir):
+    """sg_calc_snn and sg_merge_graphs against the reference's calc_snn and
+    merge_graphs run on the same two graphs (bit-exact), and the knn_utils
+    surface that mirrors merge_graphs."""
+    import scipy.sparse as sps
+    from scarf_gb300 import knn_utils
+    ref = np.load(os.path.join(golden_dir, "ref_functions.npz"))
+    n, k = int(ref["merge_n"]), int(ref["merge_k"])
+    idx = [cu(ref[f"merge_g{g}_indices"].astype(np.int64)) for g in range(2)]
+    w = [cu(ref[f"merge_g{g}_data"].reshape(n, k)) for g in range(2)]
+    snn = [K.calc_snn(i) for i in idx]
+    torch.cuda.synchronize()
+    for g in range(2):
+        assert np.array_equal(snn[g].cpu().numpy(), ref[f"merge_g{g}_snn"])
+    oi, ow = K.merge_graphs(idx, w, snn)
+    torch.cuda.synchronize()
+    assert np.array_equal(oi.cpu().numpy().ravel(), ref["merge_col"])
+    assert np.array_equal(ow.cpu().numpy().ravel(), ref["merge_data"])
+    mats = [sps.csr_matrix((ref[f"merge_g{g}_data"], ref[f"merge_g{g}_indices"].ravel(),
+                            np.arange(0, n * k + 1, k)), shape=(n, n)) for g in range(2)]
+    m = knn_utils.merge_graphs(mats)
+    assert np.array_equal(m.row, ref["merge_row"]) and np.array_equal(m.col, ref["merge_col"])
+    assert np.array_equal(m.data, ref["merge_data"])
+
+
+@pytest.mark.gpu
+def test_merge_graphs_three_graphs_with_ties(K):
+    """Three graphs with shared neighbours and tied weight + snn values (the
+    tie rule of the restatement: the later candidate first) against the oracle."""
+    rng = np.random.default_rng(11)
+    n, k = 500, 12
+    base = np.stack([rng.choice(n, k, replace=False) for _ in range(n)])
+    idx_np, w_np = [], []
+    for g in range(3):
+        mi = base.copy()
+        swap = rng.random((n, k)) < 0.4
+        mi[swap] = rng.integers(0, n, swap.sum())
+        # keep each row's neighbours distinct
+        for r in range(n):
+            _, first = np.unique(mi[r], return_index=True)
+            dup = np.setdiff1d(np.arange(k), first)
+            pool = np.setdiff1d(np.arange(n), mi[r])
+            mi[r, dup] = rng.choice(pool, len(dup), replace=False)
+        idx_np.append(mi)
+        w_np.append(np.round(rng.random((n, k)) * 4) / 4)   # quarter steps: many ties
+    idx = [cu(a.astype(np.int64)) for a in idx_np]
+    w = [cu(a) for a in w_np]
+    snn = [K.calc_snn(i) for i in idx]
+    oi, ow = K.merge_graphs(idx, w, snn)
+    torch.cuda.synchronize()
+    mats = [sp.csr_matrix((w_np[g].ravel(), idx_np[g].ravel(), np.arange(0, n * k + 1, k)), shape=(n, n))
+            for g in range(3)]
+    want = oracle.merge_graphs(mats)
+    assert np.array_equal(oi.cpu().numpy().ravel(), want.col)
+    assert np.array_equal(ow.cpu().numpy().ravel(), want.data)

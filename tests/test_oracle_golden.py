@@ -199,3 +199,22 @@ def test_kmeans_hash_is_the_splitmix64_finaliser():
         return z ^ (z >> 31)
     for seed, stream, i in ((4466, 1, 0), (0, 2, 7), ((1 << 64) - 5, 0x80000000 + 3, 4095)):
         assert int(oracle.kmeans_hash(seed, stream, i)) == ref(seed, stream, i)
+
+
+def _merge_inputs(ref):
+    n, k = int(ref["merge_n"]), int(ref["merge_k"])
+    mats = [sp.csr_matrix((ref[f"merge_g{g}_data"], ref[f"merge_g{g}_indices"].ravel(),
+                           np.arange(0, n * k + 1, k)), shape=(n, n)) for g in range(2)]
+    return n, k, mats
+
+
+def test_calc_snn_and_merge_graphs(ref):
+    """calc_snn and merge_graphs (knn_utils.py:195-274) against the reference's
+    own functions run on the same two graphs."""
+    n, k, mats = _merge_inputs(ref)
+    for g in range(2):
+        assert np.array_equal(oracle.calc_snn(ref[f"merge_g{g}_indices"]), ref[f"merge_g{g}_snn"])
+    m = oracle.merge_graphs(mats)
+    assert np.array_equal(m.row, ref["merge_row"])
+    assert np.array_equal(m.col, ref["merge_col"])
+    assert np.array_equal(m.data, ref["merge_data"])
