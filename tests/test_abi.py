@@ -58,3 +58,22 @@ def test_python_entry_points_refuse_without_gpu():
     from scarf_gb300 import kernels
     with pytest.raises(RuntimeError):
         kernels.handle()
+
+
+def _declared_arities():
+    """Parameter count of every sg_ declaration in the header."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"(sg_\w+)\s*\(([^;{]*?)\)\s*;", text, re.S):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_table_matches_header_arity():
+    """Every ctypes signature has as many arguments as its C declaration."""
+    from scarf_gb300 import _lib
+    arity = _declared_arities()
+    bad = {n: (len(args), arity.get(n)) for n, (_, args) in _lib.SIGNATURES.items() if arity.get(n) != len(args)}
+    assert not bad, bad
