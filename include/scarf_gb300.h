@@ -161,7 +161,10 @@ double sg_pca_filter_residual(const sg_handle* h);
 
 /* a5 -- the reducer ((x - mu)/sigma) . L (scarf/ann.py:129-138, :191-192):
  * scores[r*ld_s + c], c < d (columns d..ld_s-1 are written 0). bf16_out (may be
- * NULL) receives a BF16 copy with row stride ld_b (zero padded). */
+ * NULL) receives a BF16 copy with row stride ld_b (zero padded). From 4,096
+ * rows the product runs as one tensor-core GEMM (FP32 emulated with BF16
+ * splits) over x L/sigma minus a per-column shift; x must then be finite
+ * (non-finite inputs give unspecified scores rather than NaN). */
 int sg_project(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld,
                const float* mu32, const float* sigma32, const float* loadings32, int32_t d,
                int32_t ld_l, float* scores, int32_t ld_s, void* bf16_out, int32_t ld_b,
