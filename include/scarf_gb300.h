@@ -264,6 +264,21 @@ int sg_merge_graphs(sg_handle* h, int32_t n_graphs, const int64_t* const* indice
                     const double* const* snn, int64_t n, int32_t k, int64_t* out_indices, double* out_w,
                     void* stream);
 
+/* f3 -- the UMAP layout of the fused graph (scarf/umap.py:41-115: umap-learn's
+ * optimize_layout_euclidean with move_other=True, densMAP off): n_epochs
+ * epochs of attraction along the edges head[i] -> tail[i] (int32, E edges,
+ * sampled every epochs_per_sample[i] epochs; <= 0 never) and repulsion from
+ * negative_sample_rate random vertices per sample, on embedding[n_vertices x
+ * dim] float32 in place. a, b: the curve parameters (find_ab_params); gamma:
+ * repulsion strength; alpha decays linearly from initial_alpha. All edges of
+ * an epoch are processed concurrently, their steps added to the embedding
+ * atomically (reads may be stale, as in umap-learn's parallel mode), with
+ * negative samples drawn from a counter hash of `seed`. dim <= 8. */
+int sg_umap_layout(sg_handle* h, const int32_t* head, const int32_t* tail, const float* epochs_per_sample,
+                   int64_t n_edges, int64_t n_vertices, int32_t dim, float* embedding, int32_t n_epochs, float a,
+                   float b, float gamma, float initial_alpha, float negative_sample_rate, uint64_t seed,
+                   void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,6 +13,10 @@ it is restated from its published algorithm:
   (``requirements.txt:16``);
 * hnswlib 0.8.0 (``requirements.txt:3``) is *not* restated: the oracle is an
   exact FP64 kNN, which is what the GPU path is measured against;
+* umap-learn (unpinned) ``find_ab_params``, ``make_epochs_per_sample`` and
+  the single-threaded ``optimize_layout_euclidean`` (move_other=True, densMAP
+  off) that scarf's UMAP step calls, with the negative samples drawn from a
+  caller-given generator (``umap_layout_sequential``);
 * scikit-learn 1.6.1 ``MiniBatchKMeans.partial_fit`` / ``predict``
   (``sklearn/cluster/_kmeans.py``: ``_mini_batch_step``, ``_random_reassign``,
   ``_kmeans_plusplus``; ``_k_means_minibatch.pyx``: ``_minibatch_update_dense``)
@@ -48,6 +52,9 @@ __all__ = [
     "calc_snn",
     "weight_sort_indices",
     "merge_graphs",
+    "umap_find_ab_params",
+    "umap_make_epochs_per_sample",
+    "umap_layout_sequential",
     "store_to_sparse",
     "symmetrize",
     "fuzzy_simplicial_set",
@@ -737,3 +744,74 @@ def merge_graphs(csr_mats):
         data.extend(b)
     row = np.repeat(np.arange(n), nk)
     return sp.coo_matrix((data, (row, col)), shape=csr_mats[0].shape)
+
+
+# ---- f3: the UMAP layout (scarf/umap.py:41-163 over umap-learn) --------------
+
+
+def umap_find_ab_params(spread: float, min_dist: float):
+    """umap-learn find_ab_params (scipy curve_fit of 1 / (1 + a x^(2b)))."""
+    from scipy.optimize import curve_fit
+
+    def curve(x, a, b):
+        return 1.0 / (1.0 + a * x ** (2 * b))
+
+    xv = np.linspace(0, spread * 3, 300)
+    yv = np.zeros(xv.shape)
+    yv[xv < min_dist] = 1.0
+    yv[xv >= min_dist] = np.exp(-(xv[xv >= min_dist] - min_dist) / spread)
+    params, _ = curve_fit(curve, xv, yv)
+    return float(params[0]), float(params[1])
+
+
+def umap_make_epochs_per_sample(weights: np.ndarray, n_epochs: int) -> np.ndarray:
+    result = -1.0 * np.ones(weights.shape[0], dtype=np.float64)
+    n_samples = n_epochs * (weights / weights.max())
+    result[n_samples > 0] = float(n_epochs) / np.float64(n_samples[n_samples > 0])
+    return result
+
+
+def umap_layout_sequential(y: np.ndarray, head, tail, eps, n_epochs: int, a: float, b: float, gamma: float = 1.0,
+                           initial_alpha: float = 1.0, negative_sample_rate: float = 5.0, rand_vertex=None):
+    """umap-learn optimize_layout_euclidean, one thread, move_other=True:
+    edges in order every epoch (see the GPU kernel's header for the update
+    rules); ``rand_vertex(epoch, edge, p)`` draws the negative samples. Returns
+    the float32 layout (small cases only: Python loops)."""
+    y = np.array(y, dtype=np.float32)
+    nv, dim = y.shape
+    eps = np.asarray(eps, dtype=np.float64)
+    eps_neg = eps / negative_sample_rate
+    nxt = eps.copy()
+    nxt_neg = eps_neg.copy()
+    alpha = initial_alpha
+    clip = lambda v: min(4.0, max(-4.0, v))
+    for n in range(n_epochs):
+        for i in range(len(eps)):
+            if eps[i] <= 0 or nxt[i] > n:
+                continue
+            j, k = int(head[i]), int(tail[i])
+            cur, oth = y[j], y[k]
+            d2 = float(((cur - oth) ** 2).sum())
+            gc = (-2.0 * a * b * d2 ** (b - 1.0) / (a * d2 ** b + 1.0)) if d2 > 0 else 0.0
+            for d in range(dim):
+                g = clip(gc * (cur[d] - oth[d]))
+                cur[d] += g * alpha
+                oth[d] += -g * alpha
+            nxt[i] += eps[i]
+            nneg = int((n - nxt_neg[i]) / eps_neg[i])
+            for p in range(nneg):
+                kk = int(rand_vertex(n, i, p)) % nv
+                o = y[kk]
+                e2 = float(((cur - o) ** 2).sum())
+                if e2 > 0:
+                    rc = 2.0 * gamma * b / ((0.001 + e2) * (a * e2 ** b + 1.0))
+                elif j == kk:
+                    continue
+                else:
+                    rc = 0.0
+                for d in range(dim):
+                    g = clip(rc * (cur[d] - o[d])) if rc > 0 else 4.0
+                    cur[d] += g * alpha
+            nxt_neg[i] += nneg * eps_neg[i]
+        alpha = initial_alpha * (1.0 - float(n) / float(n_epochs))
+    return y

@@ -65,6 +65,7 @@ SIGNATURES = {
     "sg_kmeans_minibatch": (C.c_int, [vp, vp, i64, i32, i32, i32, i32, u64, vp, vp, vp]),
     "sg_calc_snn": (C.c_int, [vp, vp, i64, i32, vp, vp]),
     "sg_merge_graphs": (C.c_int, [vp, i32, vp, vp, vp, i64, i32, vp, vp, vp]),
+    "sg_umap_layout": (C.c_int, [vp, vp, vp, vp, i64, i64, i32, vp, i32, f32, f32, f32, f32, f32, u64, vp]),
 }
 
 _lock = threading.Lock()

@@ -308,6 +308,24 @@ def merge_graphs(indices, weights, snns):
     return out_i, out_w
 
 
+def umap_layout(head: torch.Tensor, tail: torch.Tensor, epochs_per_sample: torch.Tensor, embedding: torch.Tensor,
+                n_epochs: int, a: float, b: float, gamma: float = 1.0, initial_alpha: float = 1.0,
+                negative_sample_rate: float = 5.0, seed: int = 0) -> torch.Tensor:
+    """f3: UMAP layout epochs on ``embedding`` (n x dim float32, in place; see
+    sg_umap_layout). ``head``/``tail`` int32 edge endpoints, ``epochs_per_sample``
+    float32 per edge."""
+    _need(head, "head", torch.int32, 1)
+    _need(tail, "tail", torch.int32, 1)
+    _need(epochs_per_sample, "epochs_per_sample", torch.float32, 1)
+    _need(embedding, "embedding", torch.float32, 2)
+    dev = embedding.device
+    L.check(L.load().sg_umap_layout(handle(dev.index).ptr, _p(head), _p(tail), _p(epochs_per_sample), head.numel(),
+                                    embedding.shape[0], embedding.shape[1], _p(embedding), int(n_epochs), float(a),
+                                    float(b), float(gamma), float(initial_alpha), float(negative_sample_rate),
+                                    C.c_uint64(int(seed) & ((1 << 64) - 1)), _stream(dev)))
+    return embedding
+
+
 def fuzzy_union(edges: torch.Tensor, w: torch.Tensor, n: int, k: int, use_k: Optional[int] = None,
                 mix: float = 1.0, upper_only: bool = False) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
     """a9: CSR (indptr int64, indices int32, data float64) of the fuzzy union."""

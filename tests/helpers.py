@@ -45,3 +45,30 @@ def clustered_points(n, d, n_clusters=8, seed=0, spread=0.6, dup=()):
     for a, b in dup:
         x[b] = x[a]
     return x.astype(np.float32)
+
+
+def umap_graph(n, d, n_clusters, k, seed):
+    """Clustered points, their labels and the fused UMAP graph of their exact
+    kNN (oracle smoothing + fuzzy union) as COO arrays (head, tail, weight)."""
+    import oracle
+    rng = np.random.default_rng(seed)
+    centers = rng.normal(0, 6, size=(n_clusters, d))
+    lab = rng.integers(0, n_clusters, n)
+    x = (centers[lab] + rng.normal(size=(n, d))).astype(np.float32)
+    ki, kd = oracle.exact_knn(x, x, k + 1)
+    fi, fd, _ = oracle.fix_knn_query(ki, kd.astype(np.float32), np.arange(n))
+    edges, w = oracle.smoothen_dists(fi.astype(np.uint64), fd.astype(np.float64), 1.0, 1.5, 1000)
+    import scipy.sparse as sp
+    g = sp.csr_matrix((w, (edges[:, 0].astype(np.int64), edges[:, 1].astype(np.int64))), shape=(n, n))
+    u = oracle.fuzzy_simplicial_set(g, 1.0).tocsr()
+    u.sort_indices()
+    u = u.tocoo()
+    return x, lab, g, u.row.astype(np.int64), u.col.astype(np.int64), u.data
+
+
+def embedding_purity(y, lab, k=10):
+    """Fraction of each point's k nearest embedded neighbours in its cluster."""
+    d = ((y[:, None, :] - y[None, :, :]) ** 2).sum(-1)
+    np.fill_diagonal(d, np.inf)
+    nn = np.argsort(d, axis=1)[:, :k]
+    return float((lab[nn] == lab[:, None]).mean())

@@ -542,3 +542,49 @@ def test_merge_graphs_three_graphs_with_ties(K):
     want = oracle.merge_graphs(mats)
     assert np.array_equal(oi.cpu().numpy().ravel(), want.col)
     assert np.array_equal(ow.cpu().numpy().ravel(), want.data)
+
+
+@pytest.mark.gpu
+def test_umap_layout_matches_sequential_restatement_in_quality(K):
+    """sg_umap_layout (all edges of an epoch concurrently) against the
+    restated single-threaded optimize_layout_euclidean on the same fused graph
+    and start: both separate the clusters, and their neighbourhood purity
+    agrees within 0.08 (the two are samples of one stochastic process; the
+    concurrent epochs apply a vertex's steps from one stale position)."""
+    from helpers import umap_graph, embedding_purity
+    x, lab, _, head, tail, w = umap_graph(400, 10, 5, 10, seed=6)
+    a, b = oracle.umap_find_ab_params(2.0, 1.0)
+    eps = oracle.umap_make_epochs_per_sample(w, 60)
+    y0 = (np.random.default_rng(1).normal(size=(400, 2)) * 10).astype(np.float32)
+    y = cu(y0.copy())
+    K.umap_layout(cu(head.astype(np.int32)), cu(tail.astype(np.int32)), cu(eps.astype(np.float32)), y, 60, a, b,
+                  seed=3)
+    torch.cuda.synchronize()
+    got = y.cpu().numpy()
+    assert np.isfinite(got).all()
+    rnd = np.random.default_rng(2)
+    want = oracle.umap_layout_sequential(y0, head, tail, eps, 60, a, b,
+                                         rand_vertex=lambda n, i, p: rnd.integers(1 << 30))
+    pg, pw = embedding_purity(got, lab), embedding_purity(want, lab)
+    assert embedding_purity(y0, lab) < 0.5
+    assert pw > 0.95 and pg > 0.9
+    assert pg >= pw - 0.08
+
+
+@pytest.mark.gpu
+def test_umap_fit_transform_surface(K):
+    """scarf_gb300.umap.fit_transform (scarf/umap.py:126-163): the GPU fuzzy
+    union equals the reference's scipy union, and the layout separates the
+    clusters from scarf's default parameters."""
+    from helpers import umap_graph, embedding_purity
+    from scarf_gb300 import umap as gu
+    x, lab, g, head, tail, w = umap_graph(500, 10, 4, 10, seed=8)
+    rows, cols, vals = gu.fuzzy_simplicial_set(g, 1.0)
+    assert np.array_equal(rows.cpu().numpy(), head) and np.array_equal(cols.cpu().numpy(), tail)
+    assert np.array_equal(vals.cpu().numpy(), w)
+    y0 = (np.random.default_rng(3).normal(size=(500, 2)) * 10).astype(np.float32)
+    emb, a, b = gu.fit_transform(g, y0, 2.0, 1.0, 100, 4444, 1.0, 1.0, 5, {}, False, 1, False)
+    assert emb.shape == (500, 2) and np.isfinite(emb).all()
+    assert embedding_purity(emb, lab) > 0.9
+    with pytest.raises(NotImplementedError):
+        gu.fit_transform(g, y0, 2.0, 1.0, 10, 4444, 1.0, 1.0, 5, {"lambda": 2.0}, False, 1, False)

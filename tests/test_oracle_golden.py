@@ -218,3 +218,29 @@ def test_calc_snn_and_merge_graphs(ref):
     assert np.array_equal(m.row, ref["merge_row"])
     assert np.array_equal(m.col, ref["merge_col"])
     assert np.array_equal(m.data, ref["merge_data"])
+
+
+def test_umap_find_ab_params_published_values():
+    """umap-learn's curve parameters for its defaults (spread 1, min_dist 0.1)
+    are the published a = 1.577, b = 0.895; the GPU module's copy agrees."""
+    a, b = oracle.umap_find_ab_params(1.0, 0.1)
+    assert abs(a - 1.577) < 1e-3 and abs(b - 0.895) < 1e-3
+    from scarf_gb300 import umap as gu
+    assert np.allclose(gu.find_ab_params(2.0, 1.0), oracle.umap_find_ab_params(2.0, 1.0))
+    w = np.array([1.0, 0.5, 0.25, 0.0])
+    assert np.allclose(oracle.umap_make_epochs_per_sample(w, 200), [1.0, 2.0, 4.0, -1.0])
+    assert np.allclose(gu.make_epochs_per_sample(w, 200), [1.0, 2.0, 4.0, -1.0])
+
+
+def test_umap_layout_sequential_separates_clusters():
+    """The restated sequential layout pulls a random start apart into its
+    clusters (a property check: umap-learn is not installed to pin against)."""
+    from helpers import umap_graph, embedding_purity
+    x, lab, _, head, tail, w = umap_graph(150, 8, 3, 8, seed=4)
+    a, b = oracle.umap_find_ab_params(2.0, 1.0)
+    eps = oracle.umap_make_epochs_per_sample(w, 40)
+    y0 = np.random.default_rng(1).normal(size=(150, 2)) * 10
+    rnd = np.random.default_rng(2)
+    y = oracle.umap_layout_sequential(y0, head, tail, eps, 40, a, b, rand_vertex=lambda n, i, p: rnd.integers(1 << 30))
+    assert embedding_purity(y0, lab) < 0.6
+    assert embedding_purity(y, lab) > 0.95
