@@ -32,6 +32,30 @@ DEFAULTS = {"log_transform": True, "renormalize_subset": True, "dims": 11, "ann_
             "k": 11, "n_centroids": 1000, "local_connectivity": 1.0, "bandwidth": 1.5}
 
 
+def rescale_array(a: np.ndarray, frac: float = 0.9) -> np.ndarray:
+    """scarf/utils.py:120-140: clamp to the frac and 1 - frac quantiles of a
+    normal with the vector's (median-centred) location and standard deviation."""
+    from scipy.stats import norm
+    loc = (np.median(a) + np.median(a[::-1])) / 2
+    dist = norm(loc, np.std(a))
+    minv, maxv = dist.ppf(1 - frac), dist.ppf(frac)
+    a[a < minv] = minv
+    a[a > maxv] = maxv
+    return a
+
+
+def pca_fit_transform(x: np.ndarray, n_components: int) -> np.ndarray:
+    """scikit-learn PCA(n_components).fit_transform on a small dense matrix:
+    centred, SVD, signs by svd_flip on the components (the largest-magnitude
+    entry of each component positive), scores = centred x . components^T."""
+    xc = x - x.mean(0)
+    _, _, vt = np.linalg.svd(xc, full_matrices=False)
+    vt = vt[:n_components]
+    signs = np.sign(vt[np.arange(vt.shape[0]), np.argmax(np.abs(vt), axis=1)])
+    signs[signs == 0] = 1.0
+    return xc @ (vt * signs[:, None]).T
+
+
 class MetaData:
     """Column table of cells or features (the part of scarf/metadata.py the
     graph path reads: boolean keys, ``fetch``, ``active_index``)."""
@@ -362,6 +386,62 @@ class DataStore:
             keep = np.tile([True] * use_k + [False] * (k - use_k), n_cells)
             e, w = e[keep], w[keep]
         return sp.csr_matrix((w, (e[:, 0], e[:, 1])), shape=(n_cells, n_cells))
+
+    # -- UMAP (graph_datastore.py:427-457, :1218-1380) ---------------------------
+    @staticmethod
+    def _col_renamer(from_assay: str, cell_key: str, suffix: str) -> str:
+        """base_datastore.py:404-420."""
+        return "_".join(map(str, [from_assay, suffix] if cell_key == "I" else [from_assay, cell_key, suffix]))
+
+    def _get_ini_embed(self, from_assay: str, cell_key: str, feat_key: str, n_comps: int) -> np.ndarray:
+        """graph_datastore.py:427-457: PCA of the seeding k-means centres, each
+        component edge-trimmed by ``rescale_array``, given to every cell by its
+        cluster label."""
+        normed_loc = f"{from_assay}/normed__{cell_key}__{feat_key}"
+        reduction_loc = self.zw[normed_loc].attrs["latest_reduction"]
+        kmeans_loc = self.zw[reduction_loc].attrs["latest_kmeans"]
+        if kmeans_loc not in self.zw:
+            raise KeyError(f"{kmeans_loc} not found: the seeding k-means was not fitted")
+        pc = pca_fit_transform(np.asarray(self.zw[kmeans_loc]["cluster_centers"][:], dtype=np.float64), n_comps)
+        for i in range(n_comps):
+            pc[:, i] = rescale_array(pc[:, i])
+        clusters = np.asarray(self.zw[kmeans_loc]["cluster_labels"][:]).astype(np.uint32)
+        return np.array([pc[x] for x in clusters]).astype(np.float32, order="C")
+
+    def run_umap(self, from_assay: Optional[str] = None, cell_key: Optional[str] = None,
+                 feat_key: Optional[str] = None, symmetric_graph: Optional[bool] = False,
+                 graph_upper_only: Optional[bool] = False, ini_embed: Optional[np.ndarray] = None,
+                 umap_dims: int = 2, spread: float = 2.0, min_dist: float = 1, n_epochs: int = 300,
+                 repulsion_strength: float = 1.0, initial_alpha: float = 1.0, negative_sample_rate: float = 5,
+                 use_density_map: bool = False, dens_lambda: float = 2.0, dens_frac: float = 0.3,
+                 dens_var_shift: float = 0.1, random_seed: int = 4444, label: str = "UMAP",
+                 integrated_graph: Optional[str] = None, parallel: bool = False,
+                 nthreads: Optional[int] = None) -> None:
+        """graph_datastore.py:1218-1380 with the layout on the GPU
+        (scarf_gb300.umap.fit_transform). densMAP and integrated graphs are not
+        part of this build."""
+        from .umap import fit_transform
+        if use_density_map:
+            raise NotImplementedError("densMAP is not part of the GPU path")
+        if integrated_graph is not None:
+            raise NotImplementedError("integrated graphs are not part of the GPU path")
+        from_assay = from_assay or self._defaultAssay
+        assay = self._get_assay(from_assay)
+        cell_key = cell_key or assay.attrs.get("latest_cell_key", "I")
+        feat_key = feat_key or assay.attrs.get("latest_feat_key")
+        graph = self.load_graph(from_assay=from_assay, cell_key=cell_key, feat_key=feat_key,
+                                symmetric=symmetric_graph, upper_only=graph_upper_only)
+        if ini_embed is None:
+            ini_embed = self._get_ini_embed(from_assay, cell_key, feat_key, umap_dims)
+        t, a, b = fit_transform(graph=graph.tocoo(), ini_embed=ini_embed, spread=spread, min_dist=min_dist,
+                                n_epochs=n_epochs, random_seed=random_seed, repulsion_strength=repulsion_strength,
+                                initial_alpha=initial_alpha, negative_sample_rate=negative_sample_rate,
+                                densmap_kwds={}, parallel=parallel, nthreads=nthreads or self.nthreads,
+                                verbose=False)
+        for i in range(umap_dims):
+            self.cells.insert(self._col_renamer(from_assay, cell_key, f"{label}{i + 1}"), t[:, i], key=cell_key,
+                              overwrite=True)
+        return None
 
     # -- run_mapping (mapping_datastore.py:31-209) -----------------------------
     def run_mapping(self, target_assay: RNAassay, target_name: str, target_feat_key: str,

@@ -254,6 +254,13 @@ def main(ref_root: str):
     mg = merge_f(mats)
     out.update(merge_n=np.int64(nm), merge_k=np.int64(km), merge_row=mg.row, merge_col=mg.col, merge_data=mg.data)
 
+    # --- rescale_array (utils.py:120-140), used by _get_ini_embed ----------
+    ns = {"np": np}
+    rescale = lift(ref / "utils.py", "rescale_array", ns)
+    ra = rng.standard_t(3, size=500) * 2.0 + 1.0
+    out["rescale_in"] = ra.copy()
+    out["rescale_out"] = rescale(ra.copy())
+
     np.savez_compressed(HERE / "ref_functions.npz", **out)
     print("wrote", sorted(out))
 

@@ -170,3 +170,22 @@ def test_make_graphs_equals_one_by_one():
         from scarf_gb300 import kernels as K
         oi, oj, ov = (t.cpu().numpy() for t in K.fuzzy_union(one.edges, one.weights, one.n_cells, one.k))
         assert np.array_equal(ui, oi) and np.array_equal(uj, oj) and np.array_equal(uv, ov)
+
+
+def test_make_graph_writes_kmeans_and_run_umap(ds):
+    """make_graph writes the seeding k-means group (graph_datastore.py:958-975);
+    run_umap builds its start from it (_get_ini_embed) and writes UMAP1/UMAP2
+    for every cell (graph_datastore.py:1218-1380)."""
+    d, (indptr, indices, data, G, feat) = ds
+    red = d.zw["RNA/normed__I__hvgs"].attrs["latest_reduction"]
+    km = d.zw[red].attrs["latest_kmeans"]
+    centres = np.asarray(d.zw[km]["cluster_centers"][:])
+    labels = np.asarray(d.zw[km]["cluster_labels"][:])
+    assert centres.shape[1] == 15 and 2 <= centres.shape[0] <= 1000 and labels.shape == (1800,)
+    assert labels.min() >= 0 and labels.max() < centres.shape[0]
+    ini = d._get_ini_embed("RNA", "I", "hvgs", 2)
+    assert ini.shape == (1800, 2) and ini.dtype == np.float32
+    d.run_umap(feat_key="hvgs", n_epochs=50)
+    u1, u2 = d.cells.fetch("RNA_UMAP1"), d.cells.fetch("RNA_UMAP2")
+    assert u1.shape == (1800,) and np.isfinite(u1).all() and np.isfinite(u2).all()
+    assert np.std(u1) > 0 and np.std(u2) > 0

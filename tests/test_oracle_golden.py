@@ -244,3 +244,17 @@ def test_umap_layout_sequential_separates_clusters():
     y = oracle.umap_layout_sequential(y0, head, tail, eps, 40, a, b, rand_vertex=lambda n, i, p: rnd.integers(1 << 30))
     assert embedding_purity(y0, lab) < 0.6
     assert embedding_purity(y, lab) > 0.95
+
+
+def test_rescale_array_and_ini_embed_pca(ref):
+    """The host steps of _get_ini_embed (graph_datastore.py:427-457):
+    rescale_array against the reference's own function (utils.py:120-140),
+    and the PCA of the k-means centres against scikit-learn's PCA."""
+    from scarf_gb300 import datastore
+    assert np.array_equal(datastore.rescale_array(ref["rescale_in"].copy()), ref["rescale_out"])
+    skd = pytest.importorskip("sklearn.decomposition")
+    rng = np.random.default_rng(9)
+    c = rng.normal(size=(300, 20)) @ rng.normal(size=(20, 20))
+    ours = datastore.pca_fit_transform(c, 2)
+    theirs = skd.PCA(n_components=2).fit_transform(c)
+    assert np.abs(ours - theirs).max() < 1e-9 * max(1.0, np.abs(theirs).max())
