@@ -157,18 +157,20 @@ def _sklearn_minibatch(x, k, block, seed):
     return km.cluster_centers_, km.predict(x.astype(np.float64))
 
 
-def test_kmeans_minibatch_matches_sklearn_when_it_draws_nothing():
+@pytest.mark.parametrize("n,d,k,clusters,seed", [(1500, 10, 500, 12, 5), (1000, 12, 300, 9, 11)])
+def test_kmeans_minibatch_matches_sklearn_when_it_draws_nothing(n, d, k, clusters, seed):
     """k = block rows: k-means++ picks every row of the first block (in a
     random order) and no centre is ever light enough to be reassigned, so
     scikit-learn's MiniBatchKMeans is deterministic up to the order of its
-    centres, and the restatement reproduces it exactly."""
+    centres, and the restatement reproduces it exactly (the second case ends
+    on a ragged block of 100 rows)."""
     from helpers import clustered_points
-    x = clustered_points(1500, 10, n_clusters=12, seed=5)
-    c_o, l_o = oracle.kmeans_minibatch(x, 500, 500, 4466)
-    c_s, l_s = _sklearn_minibatch(x, 500, 500, 4466)
+    x = clustered_points(n, d, n_clusters=clusters, seed=seed)
+    c_o, l_o = oracle.kmeans_minibatch(x, k, k, 4466)
+    c_s, l_s = _sklearn_minibatch(x, k, k, 4466)
     d = ((c_o[:, None, :] - c_s[None, :, :]) ** 2).sum(-1)
     perm = d.argmin(1)
-    assert len(np.unique(perm)) == 500
+    assert len(np.unique(perm)) == k
     assert np.sqrt(d.min(1)).max() == 0.0
     assert np.array_equal(perm[l_o], l_s)
 
