@@ -624,7 +624,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--mode", default="full", choices=["full", "step", "serve", "knn", "union", "batched"],
+    ap.add_argument("--mode", default="full", choices=["full", "step", "serve", "knn", "union", "batched", "umap"],
                     help="step: warm-up steps then one make_graph step and nothing else (for profilers); "
                          "serve: the mapping service's latency under a Poisson request stream")
     ap.add_argument("--form", default="precision", choices=["precision", "plain"], help="form used by --mode step")
@@ -645,6 +645,8 @@ def main():
         run_union(args, cfg)
     elif args.mode == "batched":
         run_batched(args)
+    elif args.mode == "umap":
+        run_umap_layout(args)
     else:
         run_gb300(args, cfg)
 
@@ -742,6 +744,43 @@ def run_serve(args):
         "recall_at_k_sampled_request": round(rec, 5), "data": "synthetic",
         "config": {"workload": c["name"], "arrival_rate_hz": c["rate_hz"], "max_batch_rows": c["max_batch_rows"],
                    "workers": 2, "form": "precision"}}), flush=True)
+
+
+def run_umap_layout(args):
+    """The UMAP layout alone (f3 case): seeded clustered points (20 centres,
+    d = 50, N(0, 1) offsets) of --knn-refs rows, their precision self-kNN
+    (k = 21), smoothing and fuzzy union, then 300 layout epochs of a random 2-D
+    start, timed with CUDA events after a 10-epoch warm-up."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from scarf_gb300 import kernels as K
+    from scarf_gb300 import umap as gu
+    dev = torch.device("cuda", 0)
+    n, d, k = args.knn_refs, 50, 21
+    g = torch.Generator(device="cuda").manual_seed(3)
+    centers = torch.randn((20, d), generator=g, device=dev) * 4.0
+    lab = torch.randint(0, 20, (n,), generator=g, device=dev)
+    x = torch.zeros((n, 52), device=dev)
+    x[:, :d] = centers[lab] + torch.randn((n, d), generator=g, device=dev)
+    idx, dist, _ = K.knn(x, x, d, k, self_offset=0, margin=16, precision="precision")
+    edges, w = K.smooth(idx, dist, 1.0, 1.5, BATCH)
+    ip, ind, dat = K.fuzzy_union(edges, w, n, k)
+    nnz = int(ip[-1].item())
+    rows = torch.repeat_interleave(torch.arange(n, device=dev, dtype=torch.int32), ip[1:] - ip[:-1])
+    cols = ind[:nnz].contiguous()
+    eps = torch.from_numpy(gu.make_epochs_per_sample(dat[:nnz].cpu().numpy(), 300).astype(np.float32)).to(dev)
+    a, b = gu.find_ab_params(2.0, 1.0)
+    y = (torch.randn((n, 2), generator=g, device=dev) * 10).contiguous()
+    K.umap_layout(rows, cols, eps, y.clone(), 10, a, b, seed=1)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    K.umap_layout(rows, cols, eps, y, 300, a, b, seed=1)
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"mode": "umap", "cells": n, "edges": nnz, "epochs": 300,
+                      "layout_ms": round(e0.elapsed_time(e1), 3), "finite": bool(torch.isfinite(y).all().item())}))
 
 
 def run_knn(args):
