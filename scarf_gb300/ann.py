@@ -264,8 +264,8 @@ class AnnStream:
         if do_kmeans_fit is False:
             return None
         try:
-            centers, labels = K.kmeans(self.scores, self.dims, int(self.nClusters), int(self.batchSize),
-                                       int(self.randState))
+            seed = 0 if self.randState is None else int(self.randState)
+            centers, labels = K.kmeans(self.scores, self.dims, int(self.nClusters), int(self.batchSize), seed)
         except ValueError as e:  # sizes outside the kernel's limits: the seeding labels stay -1
             log.warning(f"k-means seeding skipped: {e}")
             return None
