@@ -65,6 +65,18 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(ms: float, device) -> float:
+    """The job's step time: the slowest rank's (all-reduce MAX over the
+    process group; the rank's own time outside one)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ---------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
@@ -373,10 +385,7 @@ def run_gb300(args, cfg):
                 if c:
                     eig_parts[name] = {"ms_per_step": round(t / steps, 3), "calls_per_step": c / steps}
             K.profile(False)
-        if ws > 1:
-            t = torch.tensor([ms], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, dev)
         return ms, res, launches, prof_ms, outs
 
     eig_parts = {}

@@ -72,3 +72,17 @@ def embedding_purity(y, lab, k=10):
     np.fill_diagonal(d, np.inf)
     nn = np.argsort(d, axis=1)[:, :k]
     return float((lab[nn] == lab[:, None]).mean())
+
+
+def multirank_worker(rank, ws, port, q):
+    """One rank of a CPU (gloo) process group: reports bench.max_over_ranks of
+    a rank-dependent step time."""
+    import os
+    import torch
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws))
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    import bench
+    q.put((rank, bench.max_over_ranks(10.0 + rank, torch.device("cpu")), bench.dist_env()))
+    dist.barrier()
+    dist.destroy_process_group()
