@@ -309,6 +309,61 @@ def fp64_truth(K, pipeline, ip, ind, dat, G, feat, dims, k, results, n_sample=20
     return out
 
 
+def host_link(dev, nbytes=2 << 30, reps=3):
+    """Pinned host <-> device copy bandwidth of this machine: one large copy each
+    way (a single cudaMemcpyAsync of a pinned buffer), best of ``reps``,
+    timed with CUDA events on the copying stream."""
+    import torch
+    hbuf = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    dbuf = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    st = torch.cuda.current_stream()
+    out = {"bytes": nbytes}
+    for name, (dst, src) in (("h2d_gbs", (dbuf, hbuf)), ("d2h_gbs", (hbuf, dbuf))):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            dst.copy_(src, non_blocking=True)
+            e1.record(st)
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        out[name] = round(nbytes / (best * 1e-3) / 1e9, 1)
+    del hbuf, dbuf
+    return out
+
+
+def datastore_e2e(csr, feat, cfg, reps=2):
+    """``DataStore.make_graph`` (the drop-in surface) from host numpy CSR to
+    the store's u8/f8 datasets, precision form, wall clock with the device
+    synchronised on both sides; a fresh DataStore per call so nothing is
+    cached. It includes what the reference's make_graph also does beyond the
+    timed step: the k-means seeding and the host-side dataset writes."""
+    import gc
+    import torch
+    from scarf_gb300.datastore import DataStore
+    mask = np.zeros(csr.n_genes, dtype=bool)
+    mask[feat] = True
+    times = []
+    for i in range(reps + 1):
+        ds = DataStore(csr.indptr, csr.indices, csr.data, csr.n_genes, precision="precision")
+        ds.RNA.feats.insert("I__hvgs", mask)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ds.make_graph(feat_key="hvgs", dims=cfg["dims"], k=cfg["k"], batch_size=BATCH)
+        torch.cuda.synchronize()
+        if i:
+            times.append(time.perf_counter() - t0)
+        del ds
+        gc.collect()
+        torch.cuda.empty_cache()
+    ms = statistics.median(times) * 1e3
+    return {"value": round(csr.n_cells / (ms * 1e-3), 1), "unit": "cells/s", "ms_per_step": round(ms, 1),
+            "calls": reps, "note": "DataStore.make_graph from host numpy CSR to the store's datasets (indices u8, "
+            "distances f8, edges u8, weights f8, the k-means group), wall clock"}
+
+
 def run_gb300(args, cfg):
     import torch
     import torch.distributed as dist
@@ -454,6 +509,19 @@ def run_gb300(args, cfg):
                 "work_per_launch": amount}
     h2d = int(ip_h.numel() * 8 + ind_h.numel() * 4 + dat_h.numel() * 4)
     d2h = int(sum(v.numel() * v.element_size() for v in outs.values()))
+    del outs, res_h
+    link = host_link(dev)
+    # the step cannot beat the larger of its device time and its copies at the link's rate
+    bound_ms = max(ms, h2d / (link["h2d_gbs"] * 1e9) * 1e3 + d2h / (link["d2h_gbs"] * 1e9) * 1e3)
+    ds_e2e = None if args.no_datastore else datastore_e2e(csr, feat, cfg)
+    serving = None
+    if not args.no_serve:
+        sv = serve_measure()
+        serving = {k_: sv[k_] for k_ in ("p50_ms", "p99_ms", "p50_ms_requests_le_10k_cells",
+                                          "p99_ms_requests_le_10k_cells", "requests", "cells", "cells_per_s",
+                                          "gpu_batches", "batch_ms_p50", "batch_ms_p99",
+                                          "recall_at_k_sampled_request")}
+        serving["config"] = sv["config"]["workload"]
     cells = n * ws
     line = {
         "metric": "make_graph cells/s",
@@ -488,13 +556,18 @@ def run_gb300(args, cfg):
         "eigensolver": eig,
         "kmeans": kmeans_info,
         "e2e": {"value": round(cells / (e2e_ms * 1e-3), 1), "unit": "cells/s", "ms_per_step": round(e2e_ms, 3),
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "host_link": link,
+                "bound_ms": round(bound_ms, 3), "frac_of_bound": round(bound_ms / e2e_ms, 4),
+                "call": "pipeline.make_graph on pinned host CSR (chunks of %s cells), outputs read back"
+                        % (chunk or "8ths of the")},
+        "e2e_datastore": ds_e2e,
+        "serving": serving,
         "roofline": roof,
         "clocks": clocks,
         "gpu_launches": int(launches),
     }
     if rank == 0 and ws == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(csr, feat, cfg, res, big=True)
+        line["cpu_baseline"] = cpu_baseline(cfg, device=dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -543,84 +616,109 @@ def eigensolver_comparison(K, pipeline, ip, ind, dat, G, feat, n, dims, reps=3):
 
 
 # ---------------------------------------------------------------------------
-def cpu_reference_times(csr, feat, cfg, rows=2000, ipca_blocks=1, queries=100, seed=0, ref_scores=None):
-    """Per-stage wall times of the CPU restatement on a bounded sample,
-    extrapolated to the whole workload by each stage's cost model (linear in
-    cells for normalisation, statistics, PCA blocks, projection and
-    smoothing; queries x all references for the exact kNN)."""
+CPU_SAMPLE_CELLS = 10_000
+
+
+def cpu_sample(cfg, n_cells=None, device=None):
+    """A bounded sample of the workload for the CPU legs: ``n_cells`` cells
+    drawn from the same seeded populations (genes, clusters, library sizes),
+    with their own top-variance HVGs. At C1 the sample is the whole workload."""
+    from scarf_gb300 import synth
+    n = min(cfg["n_cells"], n_cells or CPU_SAMPLE_CELLS)
+    csr = synth.nb_counts(n, cfg["n_genes"], cfg["n_clusters"], SEED, lib_median=cfg["lib_median"],
+                          device=device or "cpu", chunk=4096)
+    return csr, synth.select_hvgs(csr, cfg["n_hvg"])
+
+
+def cpu_make_graph(csr, feat, cfg):
+    """One make_graph of ``csr`` by the CPU restatement of the reference path
+    (the oracle): normalise, z-statistics, the reference's IncrementalPCA in
+    its block order, the reducer, self-kNN with the self fix (exact numpy kNN
+    standing in for hnswlib) and smoothing, each stage timed. Returns
+    ``(seconds, {stage: seconds})``."""
     import oracle
-    n, G, dims, k = csr.n_cells, csr.n_genes, cfg["dims"], cfg["k"]
-    rows = min(rows, n)
+    dims, k = cfg["dims"], cfg["k"]
     t = {}
-    p = csr.indptr[:rows + 1]
     t0 = time.perf_counter()
-    x, _ = oracle.normed_csr(p, csr.indices[:p[-1]], csr.data[:p[-1]], G, feat)
+    x, _ = oracle.normed_csr(csr.indptr, csr.indices, csr.data, csr.n_genes, feat)
     mu, sg = oracle.zstats(x)
-    t["normalise+stats"] = (time.perf_counter() - t0) * n / rows
-    z = (x - mu) / sg
-    pca = oracle.IncrementalPCARestated(dims + 1)
-    nb = max(1, min(ipca_blocks, rows // BATCH))
+    t["normalise+stats"] = time.perf_counter() - t0
     t0 = time.perf_counter()
-    for b in range(nb):
-        pca.partial_fit(z[b * BATCH:(b + 1) * BATCH])
-    t["pca (IncrementalPCA blocks)"] = (time.perf_counter() - t0) * (n / BATCH) / nb
-    load = pca.components_[:-1].T
+    z = (x - mu) / sg
+    blocks = [z[a:a + BATCH] for a in range(0, z.shape[0], BATCH)]
+    load, _ = oracle.fit_pca_reference_order(blocks, dims)
+    t["pca (IncrementalPCA)"] = time.perf_counter() - t0
     t0 = time.perf_counter()
     s = oracle.reducer(x, mu, sg, load)
-    t["projection x2"] = 2 * (time.perf_counter() - t0) * n / rows
-    if ref_scores is None:
-        rng = np.random.default_rng(seed)
-        ref_scores = rng.normal(size=(n, dims)).astype(np.float32)
-    q = np.asarray(ref_scores[:queries], dtype=np.float64)
+    t["projection"] = time.perf_counter() - t0
     t0 = time.perf_counter()
-    ki, kd = oracle.exact_knn(q, ref_scores, k + 1)
-    fi, fd, _ = oracle.fix_knn_query(ki, kd.astype(np.float32), np.arange(queries))
-    t["exact kNN (stand-in for hnswlib)"] = (time.perf_counter() - t0) * n / queries
+    ki, kd, _ = oracle.self_query_knn(s, k, BATCH)
+    t["exact kNN (stand-in for hnswlib)"] = time.perf_counter() - t0
     t0 = time.perf_counter()
-    oracle.smoothen_dists(fi.astype(np.uint64), fd.astype(np.float64), 1.0, 1.5, BATCH)
-    t["smoothing"] = (time.perf_counter() - t0) * n / queries
-    return t, s
+    oracle.smoothen_dists(ki, kd, 1.0, 1.5, BATCH)
+    t["smoothing"] = time.perf_counter() - t0
+    return sum(t.values()), t
 
 
-def cpu_baseline(csr, feat, cfg, res=None, big=False):
-    ref = None
-    if res is not None:
-        ref = res.scores[:, :res.dims].float().cpu().numpy()
-    kw = dict(rows=10_000, ipca_blocks=4, queries=1000) if big else dict(rows=2000, ipca_blocks=1, queries=100)
-    t, _ = cpu_reference_times(csr, feat, cfg, ref_scores=ref, **kw)
-    total = sum(t.values())
-    return {"value": round(csr.n_cells / total, 2), "unit": "cells/s", "cores": os.cpu_count(),
-            "kind": "port",
-            "sample": (f"oracle (numpy/scipy restatement) on {kw['rows']} cells for normalise/stats/projection, "
-                       f"{kw['ipca_blocks']} IncrementalPCA blocks of {BATCH}, {kw['queries']} exact-kNN queries "
-                       f"against all {csr.n_cells} references, smoothing of those rows; each stage scaled to "
-                       f"{csr.n_cells} cells; BLAS on all cores, the rest single-threaded numpy"),
-            "stage_seconds_projected": {k_: round(v, 3) for k_, v in t.items()}}
+def projected_cells_per_s(stage_s, n_sample, n_full):
+    """The full workload's cells/s projected from one sample's stage times:
+    every stage linear in cells, the exact kNN quadratic. A projection, not a
+    measurement."""
+    f = n_full / n_sample
+    tot = sum(v * f for k_, v in stage_s.items() if not k_.startswith("exact kNN"))
+    tot += sum(v * f * f for k_, v in stage_s.items() if k_.startswith("exact kNN"))
+    return round(n_full / tot, 2)
+
+
+def cpu_baseline(cfg, device=None):
+    csr, feat = cpu_sample(cfg, device=device)
+    cpu_make_graph(csr, feat, cfg)                    # warm-up (BLAS threads, page faults)
+    secs, stages = cpu_make_graph(csr, feat, cfg)
+    whole = csr.n_cells == cfg["n_cells"]
+    return {"value": round(csr.n_cells / secs, 2), "unit": "cells/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": (f"the whole workload ({csr.n_cells} cells)" if whole else
+                       f"make_graph of a {csr.n_cells}-cell sample drawn from the workload's populations "
+                       f"({cfg['n_genes']} genes, {cfg['n_hvg']} HVGs, {cfg['dims']} PCs, k={cfg['k']}), "
+                       f"measured") + "; oracle restatement: numpy/scipy, scikit-learn-order IncrementalPCA, "
+                       "exact numpy kNN standing in for hnswlib; BLAS on all cores, the rest single-threaded",
+            "seconds": round(secs, 3), "stage_seconds": {k_: round(v, 3) for k_, v in stages.items()},
+            "projected_full_workload_cells_per_s": None if whole else
+            projected_cells_per_s(stages, csr.n_cells, cfg["n_cells"])}
 
 
 def run_reference(args, cfg):
+    """The reference arm: the CPU restatement of the reference path (the
+    oracle) on the host cores. Each step is one whole make_graph of a bounded
+    sample of the workload (10,000 cells; at C1 the whole workload), timed by
+    the wall clock; ``value`` is that sample's cells/s as measured."""
     ws, rank, local = dist_env()
     if rank != 0:
         return
     import torch
-    dev = "cuda" if torch.cuda.is_available() else "cpu"
-    csr, feat = make_input(cfg, dev)
-    vals = []
+    csr, feat = cpu_sample(cfg, device="cuda" if torch.cuda.is_available() else "cpu")
+    secs, stages = [], None
     for i in range(args.warmup + args.steps):
-        t, _ = cpu_reference_times(csr, feat, cfg, seed=i)
+        t, st = cpu_make_graph(csr, feat, cfg)
         if i >= args.warmup:
-            vals.append(sum(t.values()))
-    total = statistics.median(vals)
-    v = round(csr.n_cells / total, 2)
+            secs.append(t)
+            stages = st
+    med = statistics.median(secs)
+    v = round(csr.n_cells / med, 2)
+    whole = csr.n_cells == cfg["n_cells"]
+    sample = (f"the whole workload ({csr.n_cells} cells) per step" if whole else
+              f"per step one make_graph of a {csr.n_cells}-cell sample drawn from the workload's populations")
     print(json.dumps({
         "impl": "reference", "metric": "make_graph cells/s", "value": v, "unit": "cells/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total * 1e3, 1), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (same seeded input)",
-        "config": {"workload": cfg["name"], "form": "reference CPU restatement"},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(med * 1e3, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (same seeded populations)",
+        "config": {"workload": cfg["name"], "form": "reference CPU restatement (oracle)", "sample_cells":
+                   csr.n_cells},
         "cpu_baseline": {"value": v, "unit": "cells/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": "per step: 2000 cells normalise/stats/projection, 1 IncrementalPCA block, "
-                                   "100 exact-kNN queries against all references, smoothing of those rows; "
-                                   "scaled to the full workload"},
+                         "sample": sample + "; numpy/scipy, scikit-learn-order IncrementalPCA, exact numpy kNN "
+                                   "standing in for hnswlib; BLAS on all cores"},
+        "stage_seconds": {k_: round(x, 3) for k_, x in stages.items()},
+        "projected_full_workload_cells_per_s": None if whole else
+        projected_cells_per_s(stages, csr.n_cells, cfg["n_cells"]),
         "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -631,8 +729,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the C4 serving figures in the default line")
+    ap.add_argument("--no-datastore", action="store_true", help="skip the DataStore.make_graph e2e figure")
     ap.add_argument("--mode", default="full", choices=["full", "step", "serve", "knn", "union", "batched", "umap"],
                     help="step: warm-up steps then one make_graph step and nothing else (for profilers); "
                          "serve: the mapping service's latency under a Poisson request stream")
@@ -669,9 +769,18 @@ SERVE = dict(name="C4: mapping service over a device-resident 500,000-cell refer
 
 def run_serve(args):
     """p50/p99 request latency and cells/s of the continuous-batching mapper."""
-    import torch
     import __graft_entry__
     __graft_entry__.build()
+    print(json.dumps(serve_measure()), flush=True)
+
+
+def serve_measure():
+    """The C4 serving workload: a 500,000-cell reference built by make_graph
+    and kept on the device, 120 Poisson-arriving requests of log-uniform
+    100-50,000 cells through MappingServer; latency percentiles, cells/s,
+    batch and upload timings, and the recall of one request against exact
+    FP64 kNN."""
+    import torch
     from scarf_gb300 import pipeline, synth
     from scarf_gb300.serving import MappingServer, Reference, latency_summary
     c = SERVE
@@ -734,7 +843,7 @@ def run_serve(args):
     got = torch.from_numpy(qi).to(dev)
     dg = ((qs[:, None, :] - rs[got]) ** 2).sum(-1)
     rec = float((dg <= kth[:, None] * (1 + 1e-6) + 1e-12).double().mean().item())
-    print(json.dumps({
+    out = {
         "metric": "mapping latency p99 (ms)", "value": round(summ["p99_ms"], 3), "unit": "ms",
         "higher_is_better": False, "p50_ms": round(summ["p50_ms"], 3), "p99_ms": round(summ["p99_ms"], 3),
         "p99_ms_requests_le_10k_cells": round(small.get("p99_ms", float("nan")), 3),
@@ -752,7 +861,10 @@ def run_serve(args):
                             for u in sorted(ulog.tolist(), key=lambda u: -(u[3] + u[4]))[:4]],
         "recall_at_k_sampled_request": round(rec, 5), "data": "synthetic",
         "config": {"workload": c["name"], "arrival_rate_hz": c["rate_hz"], "max_batch_rows": c["max_batch_rows"],
-                   "workers": 2, "form": "precision"}}), flush=True)
+                   "workers": 2, "form": "precision"}}
+    del g, ref, pool
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_umap_layout(args):

@@ -75,6 +75,18 @@ int sg_profile(sg_handle* h, int enable);
 int sg_set_autotune(sg_handle* h, int enable);
 int sg_knn_last_splits(const sg_handle* h);
 int sg_profile_reset(sg_handle* h);
+
+/* Bounded-wait test hooks (no reference counterpart). Every mbarrier wait of
+ * the tensor-core kernels gives up after a number of polls (2^22 by default),
+ * raises the kernel's error flag, lets the CTA's own copies and MMAs finish,
+ * frees its tensor memory and returns; the call then returns SG_ERR_TIMEOUT
+ * and the context stays usable. sg_set_wait_limit sets that poll limit for
+ * later calls on the handle (0 = the default). sg_test_idle_mma makes the
+ * next precision-form sg_knn on the handle launch its kernel with the MMA
+ * issuer idle, so that the copy and epilogue waits run out on a barrier that
+ * nothing arrives at; it faults nothing and leaves no work in flight. */
+int sg_set_wait_limit(sg_handle* h, uint32_t polls);
+int sg_test_idle_mma(sg_handle* h);
 int sg_profile_query(sg_handle* h, const char* name, double* total_ms, long long* count);
 
 /* a1+a3 -- library-size normalisation of CSR counts with the feature gather,
@@ -206,14 +218,16 @@ int sg_smooth(sg_handle* h, const int64_t* knn_idx, const float* knn_dist, int64
  * synchronisation, a plugin host that forbids allocations outside its
  * allocator). No counterpart in the reference: scarf never touches a device.
  * Same arguments and results as sg_smooth without a handle; runs on the
- * current device. Its scratch is a fixed array of static device memory in the
- * library (about 8.3 MB, held on every GPU that loads the library until the
- * process exits): at most 2^21 edges (n*k) and 2^14 chunks per call, larger
- * requests return SG_ERR_ARG. Nothing is allocated or freed. The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture. All calls share the one array,
- * so calls whose work overlaps on the GPU (other streams, other host threads)
- * race: order them. */
+ * current device. Its scratch (three words per chunk of rows) is a fixed
+ * array of static device memory in the library (256 KB, held on every GPU
+ * that loads the library until the process exits): at most 2^14 chunks
+ * (n / chunk_rows, rounded up) per call, larger requests return SG_ERR_ARG.
+ * Nothing is allocated or freed. The first call on a device (and the first
+ * call under a context other than the one of the last lookup) looks up the
+ * array's device address with cudaGetSymbolAddress; make that first call
+ * before any stream capture. A device reset between calls is not supported.
+ * All calls share the one array, so calls whose work overlaps on the GPU
+ * (other streams, other host threads) race: order them. */
 int sg_smooth_noalloc(const int64_t* knn_idx, const float* knn_dist, int64_t n, int32_t k,
                       double local_connectivity, double bandwidth, int64_t chunk_rows,
                       int64_t* edges_out, double* w_out, void* stream);
@@ -226,7 +240,8 @@ int sg_smooth_noalloc(const int64_t* knn_idx, const float* knn_dist, int64_t n, 
  * graph_datastore.py:1052-1055). FP64 with the reference's operation order,
  * so values are bit-identical to scipy's. Output CSR with sorted column
  * indices: indptr_out[n+1] (int64; indptr_out[n] is the nnz), indices_out and
- * data_out with room for `capacity` entries (2*nnz always suffices). */
+ * data_out with room for `capacity` entries (2*nnz always suffices).
+ * nnz < 2^30. */
 int sg_fuzzy_union(sg_handle* h, const int64_t* edges, const double* w, int64_t nnz, int64_t n,
                    int32_t k, int32_t use_k, double mix, uint32_t flags, int64_t* indptr_out,
                    int32_t* indices_out, double* data_out, int64_t capacity, void* stream);

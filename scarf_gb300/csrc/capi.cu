@@ -139,6 +139,18 @@ int sg_set_autotune(sg_handle* h, int enable) {
 
 int sg_knn_last_splits(const sg_handle* h) { return h ? h->last_knn_splits : 0; }
 
+int sg_set_wait_limit(sg_handle* h, uint32_t polls) {
+  if (!h) return sg::fail(SG_ERR_ARG, "null sg_handle");
+  h->wait_limit = polls;
+  return SG_OK;
+}
+
+int sg_test_idle_mma(sg_handle* h) {
+  if (!h) return sg::fail(SG_ERR_ARG, "null sg_handle");
+  h->idle_mma_once = true;
+  return SG_OK;
+}
+
 int sg_profile(sg_handle* h, int enable) {
   if (!h) return sg::fail(SG_ERR_ARG, "null sg_handle");
   cudaSetDevice(h->device);

@@ -33,6 +33,11 @@ struct sg_handle {
   };
   std::vector<KnnTune> knn_tune;
   int last_knn_splits = 0;
+  // bounded-wait test hooks (sg_set_wait_limit, sg_test_idle_mma): the poll
+  // limit of the tensor-core kernels' mbarrier waits (0 = the default), and a
+  // one-shot switch that keeps the next precision kNN's MMA issuer idle
+  uint32_t wait_limit = 0;
+  bool idle_mma_once = false;
   // kernel timing (off unless sg_profile(h, 1)): events around named launches
   bool prof = false;
   struct ProfRec {

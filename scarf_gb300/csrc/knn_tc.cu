@@ -112,7 +112,7 @@ template <int KC, bool SHARE>
 __global__ void __launch_bounds__(THREADS, 1)
 knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const float* __restrict__ rn, int64_t nr, int64_t rps, int* __restrict__ cand, int64_t nq_pad,
-              int fold, unsigned* __restrict__ qbound, int* __restrict__ err) {
+              int fold, unsigned* __restrict__ qbound, int* __restrict__ err, uint32_t wait_limit, int idle_mma) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = su32(smem_raw);
   uint8_t* sm = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -165,7 +165,7 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       for (int t = 0; t < ntiles; ++t) {
         const int s = t % STAGES;
         const uint32_t ph = (t / STAGES) & 1;
-        if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) break;
+        if (!mbar_wait(&empty[s], ph ^ 1u, err, 1, wait_limit)) break;
         mbar_expect_tx(&full[s], B_BYTES);
         tma_load_2d(sB + s * B_BYTES, &tmB, &full[s], 0, int(s_begin + int64_t(t) * BN));
         ++issued;
@@ -181,9 +181,9 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       }
     }
   } else if (warp == 1) {
-    if (lane == 0) {
+    if (lane == 0 && !idle_mma) {
       int issued = 0;
-      if (mbar_wait(a_full, 0, err, 2)) {
+      if (mbar_wait(a_full, 0, err, 2, wait_limit)) {
         tc_fence_after();
         const uint64_t adesc0 = smem_desc_sw128(su32(sA));
         const uint64_t adesc1 = smem_desc_sw128(su32(sA + A_TILE_BYTES));
@@ -192,8 +192,8 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
           const uint32_t ph = (t / STAGES) & 1;
           const int b = t & 1;
           const uint32_t aph = (t >> 1) & 1;
-          if (!mbar_wait(&acc_empty[b], aph ^ 1u, err, 3)) break;
-          if (!mbar_wait(&full[s], ph, err, 4)) break;
+          if (!mbar_wait(&acc_empty[b], aph ^ 1u, err, 3, wait_limit)) break;
+          if (!mbar_wait(&full[s], ph, err, 4, wait_limit)) break;
           tc_fence_after();
           const uint64_t bdesc = smem_desc_sw128(su32(sB + s * B_BYTES));
           const uint32_t d0 = tmem + uint32_t(b) * ACC_COLS;
@@ -300,7 +300,7 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
           shared = fminf(shared, bits_key(__ldcg(qb)));
           thr = fminf(thr, shared);
         }
-        bool ok = mbar_wait(&acc_full[b], aph, err, 5);
+        bool ok = mbar_wait(&acc_full[b], aph, err, 5, wait_limit);
         ok = __all_sync(0xffffffffu, ok);
         if (!ok) return;
         tc_fence_after();
@@ -393,15 +393,18 @@ __global__ void queries_bf16_kernel(const float* __restrict__ in, int64_t n, int
 
 template <int KC>
 int launch_tc(const CUtensorMap& a, const CUtensorMap& b, const float* rn, int64_t nr, int64_t rps, int nsplit,
-              int* cand, int64_t nq_pad, int fold, unsigned* qbound, int* err, cudaStream_t st) {
+              int* cand, int64_t nq_pad, int fold, unsigned* qbound, int* err, uint32_t wait_limit, int idle_mma,
+              cudaStream_t st) {
   const size_t smem = smem_bytes(KC);
   dim3 grid(unsigned(nq_pad / BQ), unsigned(nsplit));
   if (nsplit > 1) {
     SG_CUDA(cudaFuncSetAttribute(knn_tc_kernel<KC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    knn_tc_kernel<KC, true><<<grid, THREADS, smem, st>>>(a, b, rn, nr, rps, cand, nq_pad, fold, qbound, err);
+    knn_tc_kernel<KC, true><<<grid, THREADS, smem, st>>>(a, b, rn, nr, rps, cand, nq_pad, fold, qbound, err, wait_limit,
+                                                           idle_mma);
   } else {
     SG_CUDA(cudaFuncSetAttribute(knn_tc_kernel<KC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    knn_tc_kernel<KC, false><<<grid, THREADS, smem, st>>>(a, b, rn, nr, rps, cand, nq_pad, fold, qbound, err);
+    knn_tc_kernel<KC, false><<<grid, THREADS, smem, st>>>(a, b, rn, nr, rps, cand, nq_pad, fold, qbound, err, wait_limit,
+                                                           idle_mma);
   }
   SG_LAUNCH_CHECK();
   return SG_OK;
@@ -468,13 +471,16 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   if (rc) return rc;
   rc = make_map(&tb, Rb, nr_pad, BN);
   if (rc) return rc;
+  const uint32_t wl = h->wait_limit ? h->wait_limit : WAIT_LIMIT;
+  const int idle = h->idle_mma_once ? 1 : 0;
+  h->idle_mma_once = false;
   {
   sg::ProfScope prof(h, "knn_tc", st);
-  if (kc == 16) rc = launch_tc<16>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, st);
-  else if (kc == 32) rc = launch_tc<32>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, st);
-  else if (kc == 40) rc = launch_tc<40>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, st);
-  else if (kc == 48) rc = launch_tc<48>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, st);
-  else rc = launch_tc<64>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, st);
+  if (kc == 16) rc = launch_tc<16>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, st);
+  else if (kc == 32) rc = launch_tc<32>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, st);
+  else if (kc == 40) rc = launch_tc<40>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, st);
+  else if (kc == 48) rc = launch_tc<48>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, st);
+  else rc = launch_tc<64>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, st);
   }
   if (rc) return rc;
   int herr = 0;

@@ -36,12 +36,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
 // or when another thread has already raised it. Always inlined: a call here
 // costs the single-thread TMA and MMA issuers hundreds of nanoseconds per
 // wait, which the tensor pipeline then waits for.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int* err, int code) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, int* err, int code,
+                                          uint32_t limit = WAIT_LIMIT) {
   for (uint32_t it = 0;; ++it) {
     if (mbar_try_wait(b, parity)) return true;
     if ((it & 255u) == 255u) {
       if (*reinterpret_cast<volatile int*>(err)) return false;
-      if (it >= WAIT_LIMIT) {
+      if (it >= limit) {
         atomicCAS(err, 0, code);
         return false;
       }

@@ -12,6 +12,10 @@
 //                  (a d^b + 1)), clipped, on y_j only (4 per coordinate when
 //                  d = 0 and k' != j, nothing when k' = j)
 //   alpha = initial_alpha * (1 - n / n_epochs) after epoch n.
+// The 4-per-coordinate push of a negative sample that sits exactly on the
+// head vertex is the else branch of the 0.5 line's repulsion loop; scarf's
+// requirements leave umap-learn unpinned, and a release that sets that
+// step to 0 differs only for coincident points.
 //
 // One thread per edge and epoch, all edges of an epoch concurrently. Each
 // thread follows its own copy of the head vertex through the edge's updates
@@ -27,11 +31,17 @@ namespace {
 
 constexpr int kUmapMaxDim = 8;
 
-__device__ __forceinline__ uint64_t ul_hash(uint64_t seed, uint64_t a, uint64_t b) {
-  uint64_t z = seed + (a * 0x100000000ull + b) * 0x9E3779B97F4A7C15ull;
+// SplitMix64's output function of seed + v * golden ratio
+__device__ __forceinline__ uint64_t ul_mix(uint64_t seed, uint64_t v) {
+  uint64_t z = seed + v * 0x9E3779B97F4A7C15ull;
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
   return z ^ (z >> 31);
+}
+// the draw of sample p of edge i in epoch n: one mixing round per input, so
+// no two (epoch, edge, sample) triples share a key
+__device__ __forceinline__ uint64_t ul_hash(uint64_t seed, uint64_t epoch, uint64_t edge, uint64_t p) {
+  return ul_mix(ul_mix(ul_mix(seed, epoch), edge), p);
 }
 
 __device__ __forceinline__ float clip4(float v) { return fminf(4.f, fmaxf(-4.f, v)); }
@@ -73,7 +83,7 @@ __global__ void umap_epoch_kernel(float* __restrict__ y, int dim, const int32_t*
     next[i] += eps[i];
     const int nneg = int((float(epoch) - next_neg[i]) / eps_neg[i]);
     for (int p = 0; p < nneg; ++p) {
-      const int64_t kk = int64_t(ul_hash(seed, uint64_t(epoch), uint64_t(i) * 64 + uint64_t(p)) % uint64_t(nv));
+      const int64_t kk = int64_t(ul_hash(seed, uint64_t(epoch), uint64_t(i), uint64_t(p)) % uint64_t(nv));
       const float* yo = y + kk * dim;
       float e2 = 0.f;
       for (int d = 0; d < dim; ++d) {

@@ -257,7 +257,9 @@ extern "C" int sg_fuzzy_union(sg_handle* h, const int64_t* edges, const double* 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   SG_ARG(indptr_out && (nnz == 0 || (edges && w)), "sg_fuzzy_union: null pointer argument");
   SG_ARG(n >= 1 && n < (int64_t(1) << 31), "sg_fuzzy_union: n=%lld outside [1, 2^31)", (long long)n);
-  SG_ARG(nnz >= 0 && nnz < (int64_t(1) << 32), "sg_fuzzy_union: nnz=%lld outside [0, 2^32)", (long long)nnz);
+  // per-row bucket degrees, cursors and walk counts are 32-bit: with fewer
+  // than 2^30 edges no bucket (at most 2 * nnz items) can overflow them
+  SG_ARG(nnz >= 0 && nnz < (int64_t(1) << 30), "sg_fuzzy_union: nnz=%lld outside [0, 2^30)", (long long)nnz);
   SG_ARG(k >= 1, "sg_fuzzy_union: k must be >= 1");
   if (use_k < 1) use_k = 1;
   if (use_k > k) use_k = k;
