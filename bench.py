@@ -890,7 +890,7 @@ def run_umap_layout(args):
     nnz = int(ip[-1].item())
     rows = torch.repeat_interleave(torch.arange(n, device=dev, dtype=torch.int32), ip[1:] - ip[:-1])
     cols = ind[:nnz].contiguous()
-    eps = torch.from_numpy(gu.make_epochs_per_sample(dat[:nnz].cpu().numpy(), 300).astype(np.float32)).to(dev)
+    eps = torch.from_numpy(gu.make_epochs_per_sample(dat[:nnz].cpu().numpy(), 300).astype(np.float64)).to(dev)
     a, b = gu.find_ab_params(2.0, 1.0)
     y = (torch.randn((n, 2), generator=g, device=dev) * 10).contiguous()
     K.umap_layout(rows, cols, eps, y.clone(), 10, a, b, seed=1)
@@ -920,7 +920,9 @@ def run_knn(args):
     lab = torch.randint(0, 40, (n,), generator=g, device=dev)
     refs = torch.zeros((n, ld), device=dev)
     refs[:, :d] = centers[lab] + torch.randn((n, d), generator=g, device=dev)
-    q = refs[:args.knn_queries].contiguous()
+    # the first --knn-queries rows; all rows: the self-kNN of make_graph (the
+    # same tensor as queries and references, so the locality order applies)
+    q = refs if args.knn_queries >= n else refs[:args.knn_queries].contiguous()
     self_offset = 0 if args.knn_queries <= n else -1
     for _ in range(args.warmup):
         K.knn(q, refs, d, 21, self_offset=self_offset, margin=16, precision="precision")

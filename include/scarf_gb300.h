@@ -173,14 +173,15 @@ double sg_pca_filter_residual(const sg_handle* h);
 
 /* a5 -- the reducer ((x - mu)/sigma) . L (scarf/ann.py:129-138, :191-192):
  * scores[r*ld_s + c], c < d (columns d..ld_s-1 are written 0). bf16_out (may be
- * NULL) receives a BF16 copy with row stride ld_b (zero padded). From 4,096
- * rows the product runs as one tensor-core GEMM (FP32 emulated with BF16
- * splits) over x L/sigma minus a per-column shift; x must then be finite
- * (non-finite inputs give unspecified scores rather than NaN). */
+ * NULL) receives a BF16 copy with row stride ld_b (zero padded).
+ * SG_PLAIN: FP32 SIMT products of the centred values. SG_PRECISION (d <= 64):
+ * x . (L/sigma) - mu^T (L/sigma) on the tcgen05 tensor cores, each factor split
+ * into BF16 hi + lo and the products hi.hi + hi.lo + lo.hi accumulated in FP32
+ * (about 1e-5 of the scores' scale); x must then be finite. */
 int sg_project(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld,
                const float* mu32, const float* sigma32, const float* loadings32, int32_t d,
                int32_t ld_l, float* scores, int32_t ld_s, void* bf16_out, int32_t ld_b,
-               void* stream);
+               int32_t precision, void* stream);
 
 /* a6/a7/a10 -- exact squared-L2 kNN of queries[nq x d] (row stride ld) against
  * refs[nr x d], replacing the hnswlib index (scarf/ann.py:14-28, :290-326) and
@@ -246,6 +247,77 @@ int sg_fuzzy_union(sg_handle* h, const int64_t* edges, const double* w, int64_t 
                    int32_t k, int32_t use_k, double mix, uint32_t flags, int64_t* indptr_out,
                    int32_t* indices_out, double* data_out, int64_t capacity, void* stream);
 
+/* b2 -- the mapping service (run_mapping's query, scarf/datastore/
+ * mapping_datastore.py:198-208, with align_features' fill of absent features,
+ * scarf/mapping_utils.py:148-214) as a native continuous-batching server, for
+ * hosts that are not Python. The reference is caller-owned device memory that
+ * must outlive the server: mu32/sigma32 (n_feats), loadings32 (n_feats x ld_l,
+ * the first d columns used), ref_scores (n_ref x ld_ref). The query panel is
+ * fixed per server: col_map[n_genes] maps a target gene to its reference
+ * feature or -1, missing_mask[n_feats] != 0 marks features the target lacks
+ * (filled with 1.0 after normalisation); both are host arrays, copied.
+ * norm_flags are sg_normalize_csr's; precision is the form of sg_project and
+ * sg_knn (margin 16 in the precision form). n_workers threads each own a CUDA
+ * stream, a library handle and batch buffers on `device`.
+ * Requests are admitted in arrival order while the HBM they need (rows x
+ * (normalised row + scores + results) + 8 bytes per non-zero) fits
+ * hbm_budget_bytes; one that cannot fit alone finishes with SG_ERR_BUDGET.
+ * Each batch takes up to max_batch_rows rows from the admitted requests,
+ * shortest remaining first, so large requests are served in row slices and
+ * small ones that arrive meanwhile join the next batch; a row's result does
+ * not depend on its batch. */
+typedef struct sg_server sg_server;
+int sg_serve_create(int device, const float* mu32, const float* sigma32, const float* loadings32,
+                    int32_t n_feats, int32_t d, int32_t ld_l, const float* ref_scores, int64_t n_ref,
+                    int32_t ld_ref, const int32_t* col_map, int64_t n_genes, const uint8_t* missing_mask,
+                    int32_t k, int32_t precision, double size_factor, uint32_t norm_flags,
+                    int32_t max_batch_rows, size_t hbm_budget_bytes, int32_t n_workers, sg_server** out);
+/* Queue n_rows target cells given as HOST CSR (indptr[n_rows+1] int64 with
+ * row r's entries at indices/data[indptr[r]-indptr[0] ..]); the arrays must
+ * stay valid and unchanged until the request is done. *request_id names it. */
+int sg_serve_submit(sg_server* s, const int64_t* indptr, const int32_t* indices, const int32_t* data,
+                    int64_t n_rows, int64_t* request_id);
+/* *done = 1 once the request has finished (with results or an error). */
+int sg_serve_poll(sg_server* s, int64_t request_id, int32_t* done);
+/* Block until the request is done or timeout_ms passes (SG_ERR_TIMEOUT). */
+int sg_serve_wait(sg_server* s, int64_t request_id, int64_t timeout_ms);
+/* The finished request's k nearest reference rows (idx_out, int64) and squared
+ * distances (dist_out, float32), n_rows x k host arrays; releases the request.
+ * Returns the request's own status (SG_ERR_BUDGET, a CUDA error, ...). */
+int sg_serve_result(sg_server* s, int64_t request_id, int64_t* idx_out, float* dist_out);
+/* GPU batches run and rows mapped so far (either pointer may be NULL). */
+int sg_serve_stats(sg_server* s, int64_t* batches, int64_t* rows);
+/* Stop the workers after their current batch and free the server; requests
+ * not yet done are abandoned. */
+int sg_serve_destroy(sg_server* s);
+
+/* f2 -- decoding of scarf's zarr chunks on the device: numcodecs Blosc frames
+ * (c-blosc 1.x layout, LZ4 codec, with bit shuffle, byte shuffle or none,
+ * split or whole blocks, or plain copies), as scarf's create_zarr_dataset
+ * writes them (scarf/writers.py:58-89; dense uint32 counts at :164-204).
+ * frames: HOST bytes, frame f at [frame_offsets[f], frame_offsets[f+1]);
+ * frame f decodes into the DEVICE buffer out (out_bytes long) at byte
+ * out_starts[f] (HOST array), its header's uncompressed size long. Headers are
+ * checked on the host; the LZ4 streams are decoded one warp each and the
+ * shuffles undone on the device. A malformed stream returns SG_ERR_ARG (every
+ * device read and write is bounds-checked). Synchronises the stream. */
+int sg_blosc_decode(sg_handle* h, const uint8_t* frames, const int64_t* frame_offsets, int32_t n_frames,
+                    void* out, int64_t out_bytes, const int64_t* out_starts, void* stream);
+
+/* f2 -- CSR rows of one band of decoded dense chunks (device memory): chunk k
+ * of the band (k < ceil(n_cols / chunk_cols)) is chunk_rows x chunk_cols
+ * uint32 in C order at chunks + k * chunk_rows * chunk_cols and covers
+ * columns [k * chunk_cols, ...) of a matrix n_cols wide. Rows [0, n_rows) of
+ * the band become indptr_out[n_rows + 1] (int64, starting at indptr_base) and,
+ * in ascending column order, indices_out (int32) and data_out (int32; a count
+ * above 2^31 - 1 is SG_ERR_ARG). *nnz_out receives the band's non-zeros; with
+ * capacity 0 only indptr_out and *nnz_out are written (a counting pass).
+ * Synchronises the stream. */
+int sg_chunks_to_csr(sg_handle* h, const uint32_t* chunks, int64_t n_rows, int32_t chunk_rows,
+                     int32_t chunk_cols, int64_t n_cols, int64_t indptr_base, int64_t* indptr_out,
+                     int32_t* indices_out, int32_t* data_out, int64_t capacity, int64_t* nnz_out,
+                     void* stream);
+
 /* f1 -- the MiniBatchKMeans step of make_graph (scarf/ann.py:328-346):
  * MiniBatchKMeans(n_clusters=k, random_state=seed, batch_size=block_rows)
  * partial_fit over the row blocks of x[n x d] (row stride ld, a multiple of 4)
@@ -282,17 +354,23 @@ int sg_merge_graphs(sg_handle* h, int32_t n_graphs, const int64_t* const* indice
 /* f3 -- the UMAP layout of the fused graph (scarf/umap.py:41-115: umap-learn's
  * optimize_layout_euclidean with move_other=True, densMAP off): n_epochs
  * epochs of attraction along the edges head[i] -> tail[i] (int32, E edges,
- * sampled every epochs_per_sample[i] epochs; <= 0 never) and repulsion from
+ * sampled every epochs_per_sample[i] epochs (float64, as umap-learn's
+ * make_epochs_per_sample returns them); <= 0 never) and repulsion from
  * negative_sample_rate random vertices per sample, on embedding[n_vertices x
  * dim] float32 in place. a, b: the curve parameters (find_ab_params); gamma:
- * repulsion strength; alpha decays linearly from initial_alpha. All edges of
- * an epoch are processed concurrently, their steps added to the embedding
- * atomically (reads may be stale, as in umap-learn's parallel mode), with
- * negative samples drawn from a counter hash of `seed`. dim <= 8. */
-int sg_umap_layout(sg_handle* h, const int32_t* head, const int32_t* tail, const float* epochs_per_sample,
+ * repulsion strength; alpha decays linearly from initial_alpha. The sampling
+ * schedule is kept in float64 as umap-learn keeps it. Negative samples are
+ * drawn from a counter hash of (seed, epoch, edge, sample).
+ * sequential == 0: all edges of an epoch are processed concurrently, their
+ * float32 steps added to the embedding atomically (reads may be stale, as in
+ * umap-learn's parallel mode). sequential != 0: one thread runs the loop in
+ * edge order with umap-learn's float64 gradient arithmetic on float32
+ * coordinates, deterministically (small graphs: it is the reference
+ * trajectory for tests). dim <= 8. */
+int sg_umap_layout(sg_handle* h, const int32_t* head, const int32_t* tail, const double* epochs_per_sample,
                    int64_t n_edges, int64_t n_vertices, int32_t dim, float* embedding, int32_t n_epochs, float a,
                    float b, float gamma, float initial_alpha, float negative_sample_rate, uint64_t seed,
-                   void* stream);
+                   int32_t sequential, void* stream);
 
 #ifdef __cplusplus
 }

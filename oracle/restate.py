@@ -55,6 +55,7 @@ __all__ = [
     "umap_find_ab_params",
     "umap_make_epochs_per_sample",
     "umap_layout_sequential",
+    "umap_negative_vertex",
     "store_to_sparse",
     "symmetrize",
     "fuzzy_simplicial_set",
@@ -771,12 +772,27 @@ def umap_make_epochs_per_sample(weights: np.ndarray, n_epochs: int) -> np.ndarra
     return result
 
 
+def umap_negative_vertex(seed: int, epoch: int, edge: int, p: int, nv: int) -> int:
+    """The negative sample p of edge ``edge`` in epoch ``epoch`` as the layout
+    kernel draws it: SplitMix64's output function applied once per input
+    (seed, then epoch, edge and sample number), modulo the vertex count."""
+    def mix(z, v):
+        z = (z + v * 0x9E3779B97F4A7C15) & _M64
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+        return z ^ (z >> 31)
+    return mix(mix(mix(seed & _M64, epoch), edge), p) % nv
+
+
 def umap_layout_sequential(y: np.ndarray, head, tail, eps, n_epochs: int, a: float, b: float, gamma: float = 1.0,
                            initial_alpha: float = 1.0, negative_sample_rate: float = 5.0, rand_vertex=None):
-    """umap-learn optimize_layout_euclidean, one thread, move_other=True:
-    edges in order every epoch (see the GPU kernel's header for the update
-    rules); ``rand_vertex(epoch, edge, p)`` draws the negative samples. Returns
-    the float32 layout (small cases only: Python loops)."""
+    """umap-learn optimize_layout_euclidean, one thread, move_other=True
+    (umap/layouts.py of the 0.5 line): edges in order every epoch, with the
+    arithmetic of its numba loop -- float32 coordinates and coordinate
+    differences, squared distances, gradient coefficients, alpha and the
+    sampling schedule in float64, every step rounded back to float32 when it
+    is stored. ``rand_vertex(epoch, edge, p)`` draws the negative samples.
+    Returns the float32 layout (small cases only: Python loops)."""
     y = np.array(y, dtype=np.float32)
     nv, dim = y.shape
     eps = np.asarray(eps, dtype=np.float64)
@@ -784,25 +800,34 @@ def umap_layout_sequential(y: np.ndarray, head, tail, eps, n_epochs: int, a: flo
     nxt = eps.copy()
     nxt_neg = eps_neg.copy()
     alpha = initial_alpha
-    clip = lambda v: min(4.0, max(-4.0, v))
+    clip = lambda v: min(4.0, max(-4.0, v))  # noqa: E731
+    f32 = np.float32
+
+    def sq_dist(u, v):
+        r = 0.0
+        for d in range(dim):
+            t = float(f32(u[d]) - f32(v[d]))
+            r += t * t
+        return r
+
     for n in range(n_epochs):
         for i in range(len(eps)):
             if eps[i] <= 0 or nxt[i] > n:
                 continue
             j, k = int(head[i]), int(tail[i])
             cur, oth = y[j], y[k]
-            d2 = float(((cur - oth) ** 2).sum())
+            d2 = sq_dist(cur, oth)
             gc = (-2.0 * a * b * d2 ** (b - 1.0) / (a * d2 ** b + 1.0)) if d2 > 0 else 0.0
             for d in range(dim):
-                g = clip(gc * (cur[d] - oth[d]))
-                cur[d] += g * alpha
-                oth[d] += -g * alpha
+                g = clip(gc * float(f32(cur[d]) - f32(oth[d])))
+                cur[d] = f32(float(cur[d]) + g * alpha)
+                oth[d] = f32(float(oth[d]) + (-g) * alpha)
             nxt[i] += eps[i]
             nneg = int((n - nxt_neg[i]) / eps_neg[i])
             for p in range(nneg):
                 kk = int(rand_vertex(n, i, p)) % nv
                 o = y[kk]
-                e2 = float(((cur - o) ** 2).sum())
+                e2 = sq_dist(cur, o)
                 if e2 > 0:
                     rc = 2.0 * gamma * b / ((0.001 + e2) * (a * e2 ** b + 1.0))
                 elif j == kk:
@@ -810,8 +835,8 @@ def umap_layout_sequential(y: np.ndarray, head, tail, eps, n_epochs: int, a: flo
                 else:
                     rc = 0.0
                 for d in range(dim):
-                    g = clip(rc * (cur[d] - o[d])) if rc > 0 else 4.0
-                    cur[d] += g * alpha
+                    g = clip(rc * float(f32(cur[d]) - f32(o[d]))) if rc > 0 else 4.0
+                    cur[d] = f32(float(cur[d]) + g * alpha)
             nxt_neg[i] += nneg * eps_neg[i]
         alpha = initial_alpha * (1.0 - float(n) / float(n_epochs))
     return y

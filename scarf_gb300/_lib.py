@@ -59,15 +59,25 @@ SIGNATURES = {
     "sg_knn_last_splits": (C.c_int, [vp]),
     "sg_set_wait_limit": (C.c_int, [vp, u32]),
     "sg_test_idle_mma": (C.c_int, [vp]),
-    "sg_project": (C.c_int, [vp, vp, i64, i32, i64, vp, vp, vp, i32, i32, vp, i32, vp, i32, vp]),
+    "sg_project": (C.c_int, [vp, vp, i64, i32, i64, vp, vp, vp, i32, i32, vp, i32, vp, i32, i32, vp]),
     "sg_knn": (C.c_int, [vp, vp, i64, vp, i64, i32, i32, i32, i64, i32, i32, vp, vp, vp, vp]),
     "sg_smooth": (C.c_int, [vp, vp, vp, i64, i32, f64, f64, i64, vp, vp, vp]),
     "sg_smooth_noalloc": (C.c_int, [vp, vp, i64, i32, f64, f64, i64, vp, vp, vp]),
     "sg_fuzzy_union": (C.c_int, [vp, vp, vp, i64, i64, i32, i32, f64, u32, vp, vp, vp, i64, vp]),
+    "sg_serve_create": (C.c_int, [C.c_int, vp, vp, vp, i32, i32, i32, vp, i64, i32, vp, i64, vp, i32, i32, f64, u32,
+                                  i32, sz, i32, C.POINTER(vp)]),
+    "sg_serve_submit": (C.c_int, [vp, vp, vp, vp, i64, C.POINTER(i64)]),
+    "sg_serve_poll": (C.c_int, [vp, i64, C.POINTER(i32)]),
+    "sg_serve_wait": (C.c_int, [vp, i64, i64]),
+    "sg_serve_result": (C.c_int, [vp, i64, vp, vp]),
+    "sg_serve_stats": (C.c_int, [vp, C.POINTER(i64), C.POINTER(i64)]),
+    "sg_serve_destroy": (C.c_int, [vp]),
+    "sg_blosc_decode": (C.c_int, [vp, vp, vp, i32, vp, i64, vp, vp]),
+    "sg_chunks_to_csr": (C.c_int, [vp, vp, i64, i32, i32, i64, i64, vp, vp, vp, i64, C.POINTER(i64), vp]),
     "sg_kmeans_minibatch": (C.c_int, [vp, vp, i64, i32, i32, i32, i32, u64, vp, vp, vp]),
     "sg_calc_snn": (C.c_int, [vp, vp, i64, i32, vp, vp]),
     "sg_merge_graphs": (C.c_int, [vp, i32, vp, vp, vp, i64, i32, vp, vp, vp]),
-    "sg_umap_layout": (C.c_int, [vp, vp, vp, vp, i64, i64, i32, vp, i32, f32, f32, f32, f32, f32, u64, vp]),
+    "sg_umap_layout": (C.c_int, [vp, vp, vp, vp, i64, i64, i32, vp, i32, f32, f32, f32, f32, f32, u64, i32, vp]),
 }
 
 _lock = threading.Lock()

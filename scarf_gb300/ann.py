@@ -248,7 +248,8 @@ class AnnStream:
             raise NotImplementedError("a reduction to dims >= 1 is required by the GPU path")
         self._l32 = torch.from_numpy(np.ascontiguousarray(self.loadings, dtype=np.float32)).to(dev)
         self.reducer = self._reduce
-        self.scores = K.project(self.data.x, self._mu32, self._sg32, self._l32, self.dims, n_cols=h)
+        self.scores = K.project(self.data.x, self._mu32, self._sg32, self._l32, self.dims, n_cols=h,
+                                precision=self.precision)
         if ann_idx is None:
             self.annIdx = GpuExactIndex(self.annMetric, self.dims, precision=precision, margin=margin, device=dev)
             self.annIdx._rows = [self.scores]
@@ -306,7 +307,8 @@ class AnnStream:
         t = _as_device_f32(a, self.data.x.device)
         if t.shape[1] % 4:
             t = torch.nn.functional.pad(t, (0, 4 - t.shape[1] % 4))
-        s = K.project(t, self._mu32, self._sg32, self._l32, self.dims, n_cols=self.nFeats)
+        s = K.project(t, self._mu32, self._sg32, self._l32, self.dims, n_cols=self.nFeats,
+                      precision=self.precision)
         return s[:, : self.dims].double().cpu().numpy()
 
     def transform_ann(self, a, k: Optional[int] = None, self_indices: Optional[np.ndarray] = None):

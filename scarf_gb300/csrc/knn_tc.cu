@@ -112,7 +112,8 @@ template <int KC, bool SHARE>
 __global__ void __launch_bounds__(THREADS, 1)
 knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const float* __restrict__ rn, int64_t nr, int64_t rps, int* __restrict__ cand, int64_t nq_pad,
-              int fold, unsigned* __restrict__ qbound, int* __restrict__ err, uint32_t wait_limit, int idle_mma) {
+              int fold, unsigned* __restrict__ qbound, int* __restrict__ err, uint32_t wait_limit, int idle_mma,
+              const int* __restrict__ perm, int64_t nq) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = su32(smem_raw);
   uint8_t* sm = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -134,6 +135,19 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
   const int64_t s_begin = int64_t(blockIdx.y) * rps;
   const int64_t s_end = min(nr, s_begin + rps);
   const int ntiles = int((s_end - s_begin + BN - 1) / BN);
+  // With a locality order (perm != null: queries and references are the same
+  // rows, both sorted so that neighbours sit close together), the CTA starts
+  // at the reference tile of its own queries and wraps around, so that its
+  // candidate lists fill with near neighbours first and few later keys pass.
+  int t0 = 0;
+  if (perm != nullptr && ntiles > 0) {
+    const int64_t diag = (q0 - s_begin) / BN;
+    t0 = int(diag < 0 ? 0 : (diag >= ntiles ? ntiles - 1 : diag));
+  }
+  auto tile_at = [&](int t) -> int64_t {
+    const int u = t + t0;
+    return s_begin + int64_t(u >= ntiles ? u - ntiles : u) * BN;
+  };
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -167,7 +181,7 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
         const uint32_t ph = (t / STAGES) & 1;
         if (!mbar_wait(&empty[s], ph ^ 1u, err, 1, wait_limit)) break;
         mbar_expect_tx(&full[s], B_BYTES);
-        tma_load_2d(sB + s * B_BYTES, &tmB, &full[s], 0, int(s_begin + int64_t(t) * BN));
+        tma_load_2d(sB + s * B_BYTES, &tmB, &full[s], 0, int(tile_at(t)));
         ++issued;
       }
       // on the error path, let this CTA's own copies land before leaving
@@ -294,7 +308,7 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
       for (int t = 0; t < ntiles; ++t) {
         const int b = t & 1;
         const uint32_t aph = (t >> 1) & 1;
-        const int64_t r0 = s_begin + int64_t(t) * BN;
+        const int64_t r0 = tile_at(t);
         if (kRn) reinterpret_cast<float4*>(my_rn)[lane] = __ldg(reinterpret_cast<const float4*>(rn + r0) + lane);
         if (SHARE) {
           shared = fminf(shared, bits_key(__ldcg(qb)));
@@ -335,9 +349,16 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
     else tiles(std::true_type{});
     compact();
     // list `split` of every query: nsplit lists per query
-    int* out = cand + (int64_t(blockIdx.y) * nq_pad + q0 + row) * KC;
+    // back to the caller's row order: the list of query perm[q], with the
+    // caller's reference numbers
+    const int64_t qpos = q0 + row;
+    const int64_t qout = (perm != nullptr && qpos < nq) ? int64_t(perm[qpos]) : qpos;
+    int* out = cand + (int64_t(blockIdx.y) * nq_pad + qout) * KC;
 #pragma unroll
-    for (int j = 0; j < KC; ++j) out[j] = top.i[j];
+    for (int j = 0; j < KC; ++j) {
+      const int ix = top.i[j];
+      out[j] = (perm != nullptr && ix >= 0 && ix < nr) ? perm[ix] : ix;
+    }
   }
   __syncthreads();
   if (warp == 1) {
@@ -354,13 +375,15 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
 // queries: -2 * rounded rows (exact in BF16) and, with `fold`, ones in columns
 //   d..d+2. The accumulator is then |r|^2 - 2 q.r directly.
 __global__ void refs_bf16_kernel(const float* __restrict__ in, int64_t n, int d, int ld, int fold,
-                                 __nv_bfloat16* __restrict__ out, int64_t n_pad, float* __restrict__ norms) {
+                                 __nv_bfloat16* __restrict__ out, int64_t n_pad, float* __restrict__ norms,
+                                 const int* __restrict__ perm) {
   const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (r >= n_pad) return;
   float s = 0.f;
   __nv_bfloat16* o = out + r * BK;
+  const int64_t src = (perm != nullptr && r < n) ? int64_t(perm[r]) : r;
   for (int c = 0; c < d; ++c) {
-    const __nv_bfloat16 b = __float2bfloat16_rn(r < n ? in[r * ld + c] : 0.f);
+    const __nv_bfloat16 b = __float2bfloat16_rn(r < n ? in[src * ld + c] : 0.f);
     o[c] = b;
     const float bf = __bfloat162float(b);
     s = fmaf(bf, bf, s);
@@ -380,31 +403,150 @@ __global__ void refs_bf16_kernel(const float* __restrict__ in, int64_t n, int d,
 }
 
 __global__ void queries_bf16_kernel(const float* __restrict__ in, int64_t n, int d, int ld, int fold,
-                                    __nv_bfloat16* __restrict__ out, int64_t n_pad) {
+                                    __nv_bfloat16* __restrict__ out, int64_t n_pad, const int* __restrict__ perm) {
   const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (r >= n_pad) return;
   __nv_bfloat16* o = out + r * BK;
+  const int64_t src = (perm != nullptr && r < n) ? int64_t(perm[r]) : r;
   for (int c = 0; c < d; ++c) {
-    const float v = __bfloat162float(__float2bfloat16_rn(r < n ? in[r * ld + c] : 0.f));
+    const float v = __bfloat162float(__float2bfloat16_rn(r < n ? in[src * ld + c] : 0.f));
     o[c] = __float2bfloat16_rn(-2.f * v);
   }
   for (int c = d; c < BK; ++c) o[c] = __float2bfloat16_rn((fold && c < d + 3) ? 1.f : 0.f);
 }
 
+// ---- locality order of a self-kNN ---------------------------------------
+// The rows are sorted (stably) by their nearest pilot, a strided sample of the
+// rows; queries and references then share that order, and each CTA meets its
+// own neighbourhood in its first reference tiles (see knn_tc_kernel).
+constexpr int kMaxPilots = 128;
+constexpr int kSortRows = 512;  // rows per counting-sort block
+
+// nearest pilot of every row by |p|^2 - 2 x.p (ties to the smaller pilot);
+// pilots = rows 0, stride, 2 stride, ... staged as -2p (zero padded to BK)
+__global__ void nearest_pilot_kernel(const float* __restrict__ x, int64_t n, int d, int ld, int64_t stride, int np,
+                                     int* __restrict__ pid) {
+  __shared__ float sp[kMaxPilots * BK];
+  __shared__ float pn[kMaxPilots];
+  for (int i = threadIdx.x; i < np * BK; i += blockDim.x) {
+    const int p = i / BK, c = i - p * BK;
+    sp[i] = c < d ? -2.f * x[int64_t(p) * stride * ld + c] : 0.f;
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < np; p += blockDim.x) {
+    float q = 0.f;
+    for (int c = 0; c < d; ++c) q = fmaf(sp[p * BK + c], sp[p * BK + c], q);
+    pn[p] = 0.25f * q;
+  }
+  __syncthreads();
+  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  float xr[BK];
+#pragma unroll
+  for (int c = 0; c < BK; ++c) xr[c] = c < d ? x[r * ld + c] : 0.f;
+  float best = __int_as_float(0x7f800000);
+  int bi = 0;
+  for (int p = 0; p < np; ++p) {
+    float acc = pn[p];
+#pragma unroll
+    for (int c = 0; c < BK; ++c) acc = fmaf(xr[c], sp[p * BK + c], acc);
+    if (acc < best) {
+      best = acc;
+      bi = p;
+    }
+  }
+  pid[r] = bi;
+}
+
+// rows of each counting-sort block per pilot: hist[pilot * nblk + block]
+__global__ void bin_count_kernel(const int* __restrict__ pid, int64_t n, int np, int* __restrict__ hist, int nblk) {
+  __shared__ int cnt[kMaxPilots];
+  for (int i = threadIdx.x; i < np; i += blockDim.x) cnt[i] = 0;
+  __syncthreads();
+  const int64_t a = int64_t(blockIdx.x) * kSortRows, b = min(n, a + kSortRows);
+  for (int64_t r = a + threadIdx.x; r < b; r += blockDim.x) atomicAdd(&cnt[pid[r]], 1);
+  __syncthreads();
+  for (int i = threadIdx.x; i < np; i += blockDim.x) hist[int64_t(i) * nblk + blockIdx.x] = cnt[i];
+}
+
+// exclusive scan of hist in (pilot, block) order; one CTA of 1024 threads
+__global__ void __launch_bounds__(1024) bin_scan_kernel(int* __restrict__ hist, int64_t total) {
+  __shared__ int part[1024];
+  const int64_t per = (total + 1023) / 1024;
+  const int64_t a = int64_t(threadIdx.x) * per, b = min(total, a + per);
+  int sum = 0;
+  for (int64_t i = a; i < b; ++i) sum += hist[i];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+  for (int64_t i = a; i < b; ++i) {
+    const int v = hist[i];
+    hist[i] = run;
+    run += v;
+  }
+}
+
+// stable scatter: one warp per counting-sort block, its rows 32 at a time in order
+__global__ void bin_scatter_kernel(const int* __restrict__ pid, int64_t n, int np, const int* __restrict__ off,
+                                   int nblk, int* __restrict__ perm) {
+  __shared__ int cur[kMaxPilots];
+  const int lane = threadIdx.x;
+  for (int i = lane; i < np; i += 32) cur[i] = off[int64_t(i) * nblk + blockIdx.x];
+  __syncwarp();
+  const int64_t a = int64_t(blockIdx.x) * kSortRows, b = min(n, a + kSortRows);
+  const unsigned lt = (1u << lane) - 1u;
+  for (int64_t base = a; base < b; base += 32) {
+    const int64_t r = base + lane;
+    const bool live = r < b;
+    const int p = live ? pid[r] : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, p);
+    if (live) perm[cur[p] + __popc(peers & lt)] = int(r);
+    __syncwarp();
+    if (live && (peers & lt) == 0u) cur[p] += __popc(peers);
+    __syncwarp();
+  }
+}
+
+// pilots used for n rows (0: no locality order)
+int pilots_for(int64_t n) {
+  if (n < (int64_t(1) << 15)) return 0;
+  return int(std::min<int64_t>(kMaxPilots, std::max<int64_t>(16, n / 4096)));
+}
+
+int locality_order(const float* x, int64_t n, int d, int ld, int np, int* pid, int* hist, int* perm,
+                   cudaStream_t st) {
+  const int nblk = sg::ceil_div_i(n, kSortRows);
+  nearest_pilot_kernel<<<sg::ceil_div_i(n, 128), 128, 0, st>>>(x, n, d, ld, n / np, np, pid);
+  SG_LAUNCH_CHECK();
+  bin_count_kernel<<<nblk, 256, 0, st>>>(pid, n, np, hist, nblk);
+  SG_LAUNCH_CHECK();
+  bin_scan_kernel<<<1, 1024, 0, st>>>(hist, int64_t(np) * nblk);
+  SG_LAUNCH_CHECK();
+  bin_scatter_kernel<<<nblk, 32, 0, st>>>(pid, n, np, hist, nblk, perm);
+  SG_LAUNCH_CHECK();
+  return SG_OK;
+}
+
 template <int KC>
 int launch_tc(const CUtensorMap& a, const CUtensorMap& b, const float* rn, int64_t nr, int64_t rps, int nsplit,
               int* cand, int64_t nq_pad, int fold, unsigned* qbound, int* err, uint32_t wait_limit, int idle_mma,
-              cudaStream_t st) {
+              const int* perm, int64_t nq, cudaStream_t st) {
   const size_t smem = smem_bytes(KC);
   dim3 grid(unsigned(nq_pad / BQ), unsigned(nsplit));
   if (nsplit > 1) {
     SG_CUDA(cudaFuncSetAttribute(knn_tc_kernel<KC, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     knn_tc_kernel<KC, true><<<grid, THREADS, smem, st>>>(a, b, rn, nr, rps, cand, nq_pad, fold, qbound, err, wait_limit,
-                                                           idle_mma);
+                                                           idle_mma, perm, nq);
   } else {
     SG_CUDA(cudaFuncSetAttribute(knn_tc_kernel<KC, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     knn_tc_kernel<KC, false><<<grid, THREADS, smem, st>>>(a, b, rn, nr, rps, cand, nq_pad, fold, qbound, err, wait_limit,
-                                                           idle_mma);
+                                                           idle_mma, perm, nq);
   }
   SG_LAUNCH_CHECK();
   return SG_OK;
@@ -442,13 +584,19 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   int tuned = 0;
   for (const auto& e : h->knn_tune)
     if (e.qb == qb && e.rb == rb && e.d == d && e.kc == kc) tuned = e.nsplit;
+  // self-kNN (the queries are the references): locality order of the rows
+  const int np = (queries == refs && nq == nr && self_offset == 0) ? pilots_for(nr) : 0;
+  const int nblk = np ? sg::ceil_div_i(nr, kSortRows) : 0;
   auto run = [&](int nsplit) -> int {
   const int64_t rps = sg::ceil_div(sg::ceil_div(nr, nsplit), BN) * BN;
   const int fold = d <= BK - 3 ? 1 : 0;
   const size_t need = sg::Carver::need(size_t(nr_pad) * BK * 2) + sg::Carver::need(size_t(nr_pad) * 4) +
                       sg::Carver::need(size_t(nq_pad) * BK * 2) +
                       sg::Carver::need(sizeof(int) * size_t(nsplit) * nq_pad * kc) + sg::Carver::need(sizeof(int)) +
-                      sg::Carver::need(sizeof(unsigned) * size_t(nq_pad));
+                      sg::Carver::need(sizeof(unsigned) * size_t(nq_pad)) +
+                      (np ? 2 * sg::Carver::need(sizeof(int) * size_t(nr)) +
+                                sg::Carver::need(sizeof(int) * size_t(np) * nblk)
+                          : 0);
   int status;
   void* w = sg::ws_get(h, need, &status);
   if (!w) return status;
@@ -459,12 +607,20 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   int* cand = cv.take<int>(size_t(nsplit) * nq_pad * kc);
   int* err = cv.take<int>(1);
   unsigned* qbound = cv.take<unsigned>(size_t(nq_pad));
+  int* perm = nullptr;
+  if (np) {
+    int* pid = cv.take<int>(size_t(nr));
+    perm = cv.take<int>(size_t(nr));
+    int* hist = cv.take<int>(size_t(np) * nblk);
+    const int rc0 = locality_order(refs, nr, d, ld, np, pid, hist, perm, st);
+    if (rc0) return rc0;
+  }
   SG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
   // all ones: decodes to NaN, which fminf ignores (no bound yet)
   SG_CUDA(cudaMemsetAsync(qbound, 0xFF, sizeof(unsigned) * size_t(nq_pad), st));
-  refs_bf16_kernel<<<sg::ceil_div_i(nr_pad, 256), 256, 0, st>>>(refs, nr, d, ld, fold, Rb, nr_pad, rn);
+  refs_bf16_kernel<<<sg::ceil_div_i(nr_pad, 256), 256, 0, st>>>(refs, nr, d, ld, fold, Rb, nr_pad, rn, perm);
   SG_LAUNCH_CHECK();
-  queries_bf16_kernel<<<sg::ceil_div_i(nq_pad, 256), 256, 0, st>>>(queries, nq, d, ld, fold, Qb, nq_pad);
+  queries_bf16_kernel<<<sg::ceil_div_i(nq_pad, 256), 256, 0, st>>>(queries, nq, d, ld, fold, Qb, nq_pad, perm);
   SG_LAUNCH_CHECK();
   CUtensorMap ta, tb;
   int rc = make_map(&ta, Qb, nq_pad, BQ);
@@ -476,11 +632,11 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   h->idle_mma_once = false;
   {
   sg::ProfScope prof(h, "knn_tc", st);
-  if (kc == 16) rc = launch_tc<16>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, st);
-  else if (kc == 32) rc = launch_tc<32>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, st);
-  else if (kc == 40) rc = launch_tc<40>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, st);
-  else if (kc == 48) rc = launch_tc<48>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, st);
-  else rc = launch_tc<64>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, st);
+  if (kc == 16) rc = launch_tc<16>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, perm, nq, st);
+  else if (kc == 32) rc = launch_tc<32>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, perm, nq, st);
+  else if (kc == 40) rc = launch_tc<40>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, perm, nq, st);
+  else if (kc == 48) rc = launch_tc<48>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, perm, nq, st);
+  else rc = launch_tc<64>(ta, tb, rn, nr, rps, nsplit, cand, nq_pad, fold, qbound, err, wl, idle, perm, nq, st);
   }
   if (rc) return rc;
   int herr = 0;

@@ -25,6 +25,9 @@
 #endif
 #include <vector>
 
+int sg_project_tc(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld, const float* mu32,
+                  const float* sigma32, const float* loadings32, int32_t d, int32_t ld_l, float* scores, int32_t ld_s,
+                  __nv_bfloat16* sb, int32_t ld_b, cudaStream_t st);  // proj_tc.cu
 int sg_covariance_tc(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld,
                      const float* mu32, const float* sigma32, const uint8_t* row_mask, double* cov,
                      double* zsum, cudaStream_t st);  // cov_tc.cu
@@ -336,41 +339,6 @@ project_kernel(const float* __restrict__ x, int64_t n_rows, int n_cols, int64_t 
   }
 }
 
-// The projection as one plain GEMM: ((x - mu) / sigma) L = x Lp - b with
-// Lp = L / sigma (per feature row, rounded to FP32) and b = mu^T Lp summed in
-// FP64 in a fixed order. One CTA per output column.
-__global__ void fold_loadings_kernel(const float* __restrict__ L, int h, int ld_l, const float* __restrict__ mu,
-                                     const float* __restrict__ sg, float* __restrict__ Lp, float* __restrict__ b) {
-  __shared__ double part[256];
-  const int c = blockIdx.x;
-  double acc = 0.0;
-  for (int j = threadIdx.x; j < h; j += blockDim.x) {
-    const float lp = __fdiv_rn(L[int64_t(j) * ld_l + c], sg[j]);
-    Lp[int64_t(j) * ld_l + c] = lp;
-    acc += double(mu[j]) * double(lp);
-  }
-  part[threadIdx.x] = acc;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (int(threadIdx.x) < w) part[threadIdx.x] += part[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) b[c] = float(part[0]);
-}
-
-// scores[:, c] -= b[c] for c < d, zero padding up to ld_s, optional BF16 copy
-__global__ void center_scores_kernel(float* __restrict__ s, int64_t n_rows, int d, int ld_s,
-                                     const float* __restrict__ b, __nv_bfloat16* __restrict__ sb, int ld_b) {
-  const int cols = max(ld_s, sb ? ld_b : 0);
-  const int64_t total = n_rows * cols;
-  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
-    const int64_t r = e / cols;
-    const int c = int(e - r * cols);
-    const float v = c < d ? s[r * ld_s + c] - b[c] : 0.f;
-    if (c < ld_s) s[r * ld_s + c] = v;
-    if (sb && c < ld_b) sb[r * ld_b + c] = __float2bfloat16_rn(v);
-  }
-}
 
 __global__ void pad_cols_kernel(float* __restrict__ s, int64_t n_rows, int from, int ld,
                                 __nv_bfloat16* __restrict__ sb, int from_b, int ld_b) {
@@ -1203,42 +1171,18 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
 extern "C" int sg_project(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld,
                           const float* mu32, const float* sigma32, const float* loadings32, int32_t d,
                           int32_t ld_l, float* scores, int32_t ld_s, void* bf16_out, int32_t ld_b,
-                          void* stream) {
+                          int32_t precision, void* stream) {
   SG_HANDLE_CHECK(h);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   SG_ARG(x && mu32 && sigma32 && loadings32 && scores, "sg_project: null pointer argument");
   SG_ARG(n_rows >= 0 && n_cols > 0 && ld >= n_cols && d > 0 && ld_l >= d && ld_s >= d, "sg_project: bad sizes");
   SG_ARG(!bf16_out || ld_b >= d, "sg_project: ld_b < d");
+  SG_ARG(precision == SG_PLAIN || precision == SG_PRECISION, "sg_project: unknown precision %d", precision);
   if (n_rows == 0) return SG_OK;
+  if (precision == SG_PRECISION)
+    return sg_project_tc(h, x, n_rows, n_cols, ld, mu32, sigma32, loadings32, d, ld_l, scores, ld_s,
+                         static_cast<__nv_bfloat16*>(bf16_out), ld_b, st);
   const int ccols = std::max<int>(ld_s, bf16_out ? ld_b : 0);
-  if (n_rows >= 4096) {
-    // large inputs: one GEMM on the tensor cores (FP32 emulated with BF16
-    // splits) over the uncentred rows, then the centring as a per-column shift
-    cusolverDnHandle_t sol;
-    cublasHandle_t blas;
-    int rc = solver_handles(h, st, &sol, &blas);
-    if (rc) return rc;
-    const size_t need = sg::Carver::need(sizeof(float) * size_t(n_cols) * ld_l) + sg::Carver::need(sizeof(float) * d);
-    int status;
-    void* w = sg::ws_get(h, need, &status);
-    if (!w) return status;
-    sg::Carver cv(w);
-    float* Lp = cv.take<float>(size_t(n_cols) * ld_l);
-    float* bsh = cv.take<float>(size_t(d));
-    sg::ProfScope prof(h, "project", st);
-    fold_loadings_kernel<<<d, 256, 0, st>>>(loadings32, n_cols, ld_l, mu32, sigma32, Lp, bsh);
-    SG_LAUNCH_CHECK();
-    const float one = 1.f, zero = 0.f;
-    // column-major view: scores^T (d x n, ld_s) = Lp^T (d x h, ld_l) x^T (h x n, ld)
-    SG_BLAS(cublasGemmEx(blas, CUBLAS_OP_N, CUBLAS_OP_N, d, int(n_rows), n_cols, &one, Lp, CUDA_R_32F, ld_l, x,
-                         CUDA_R_32F, int(ld), &zero, scores, CUDA_R_32F, ld_s, CUBLAS_COMPUTE_32F_EMULATED_16BFX9,
-                         CUBLAS_GEMM_DEFAULT));
-    const int64_t total = n_rows * ccols;
-    center_scores_kernel<<<unsigned(std::min<int64_t>(sg::ceil_div(total, 256), int64_t(h->sm_count) * 32)), 256, 0,
-                           st>>>(scores, n_rows, d, ld_s, bsh, static_cast<__nv_bfloat16*>(bf16_out), ld_b);
-    SG_LAUNCH_CHECK();
-    return SG_OK;
-  }
   sg::ProfScope prof(h, "project", st);
   dim3 grid(sg::ceil_div_i(n_rows, PR), sg::ceil_div_i(std::min<int>(ccols, sg::ceil_div_i(d, PC) * PC), PC));
   project_kernel<<<grid, 256, 0, st>>>(x, n_rows, n_cols, ld, mu32, sigma32, loadings32, d, ld_l, scores, ld_s,

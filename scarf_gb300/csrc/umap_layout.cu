@@ -46,8 +46,8 @@ __device__ __forceinline__ uint64_t ul_hash(uint64_t seed, uint64_t epoch, uint6
 
 __device__ __forceinline__ float clip4(float v) { return fminf(4.f, fmaxf(-4.f, v)); }
 
-__global__ void umap_init_kernel(const float* __restrict__ eps, int64_t ne, float rate, float* __restrict__ next,
-                                 float* __restrict__ next_neg, float* __restrict__ eps_neg) {
+__global__ void umap_init_kernel(const double* __restrict__ eps, int64_t ne, double rate, double* __restrict__ next,
+                                 double* __restrict__ next_neg, double* __restrict__ eps_neg) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= ne) return;
   next[i] = eps[i];
@@ -55,13 +55,18 @@ __global__ void umap_init_kernel(const float* __restrict__ eps, int64_t ne, floa
   next_neg[i] = eps_neg[i];
 }
 
+// the negative sample p of edge i in epoch n
+__device__ __forceinline__ int64_t neg_vertex(uint64_t seed, int epoch, int64_t i, int p, int64_t nv) {
+  return int64_t(ul_hash(seed, uint64_t(epoch), uint64_t(i), uint64_t(p)) % uint64_t(nv));
+}
+
 __global__ void umap_epoch_kernel(float* __restrict__ y, int dim, const int32_t* __restrict__ head,
-                                  const int32_t* __restrict__ tail, const float* __restrict__ eps,
-                                  float* __restrict__ next, float* __restrict__ next_neg,
-                                  const float* __restrict__ eps_neg, int64_t ne, int64_t nv, int epoch, float a,
+                                  const int32_t* __restrict__ tail, const double* __restrict__ eps,
+                                  double* __restrict__ next, double* __restrict__ next_neg,
+                                  const double* __restrict__ eps_neg, int64_t ne, int64_t nv, int epoch, float a,
                                   float b, float gamma, float alpha, uint64_t seed) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < ne; i += int64_t(gridDim.x) * blockDim.x) {
-    if (eps[i] <= 0.f || next[i] > float(epoch)) continue;  // edges of weight 0 never sample
+    if (eps[i] <= 0.0 || next[i] > double(epoch)) continue;  // edges of weight 0 never sample
     const int64_t j = head[i], k = tail[i];
     float* yj = y + j * dim;
     float* yk = y + k * dim;
@@ -81,9 +86,9 @@ __global__ void umap_epoch_kernel(float* __restrict__ y, int dim, const int32_t*
       atomicAdd(&yk[d], -g * alpha);
     }
     next[i] += eps[i];
-    const int nneg = int((float(epoch) - next_neg[i]) / eps_neg[i]);
+    const int nneg = int((double(epoch) - next_neg[i]) / eps_neg[i]);
     for (int p = 0; p < nneg; ++p) {
-      const int64_t kk = int64_t(ul_hash(seed, uint64_t(epoch), uint64_t(i), uint64_t(p)) % uint64_t(nv));
+      const int64_t kk = neg_vertex(seed, epoch, i, p, nv);
       const float* yo = y + kk * dim;
       float e2 = 0.f;
       for (int d = 0; d < dim; ++d) {
@@ -100,16 +105,75 @@ __global__ void umap_epoch_kernel(float* __restrict__ y, int dim, const int32_t*
         atomicAdd(&yj[d], g * alpha);
       }
     }
-    next_neg[i] += float(nneg) * eps_neg[i];
+    next_neg[i] += double(nneg) * eps_neg[i];
+  }
+}
+
+// The deterministic mode: one thread runs umap-learn's sequential loop
+// (edges in order, every update applied at once, move_other=True) with the
+// arithmetic of its numba code -- float32 coordinates and differences,
+// float64 squared distances, gradient coefficients, alpha and sampling
+// schedule -- and the same negative-sample draws as the parallel mode. For
+// small graphs: it is the reference trajectory that the parallel mode is a
+// concurrent sample of.
+__device__ __forceinline__ double sq_dist64(const float* u, const float* v, int dim) {
+  double r = 0.0;
+  for (int d = 0; d < dim; ++d) {
+    const double t = double(__fsub_rn(u[d], v[d]));
+    r = __dadd_rn(r, __dmul_rn(t, t));
+  }
+  return r;
+}
+
+__global__ void umap_sequential_kernel(float* __restrict__ y, int dim, const int32_t* __restrict__ head,
+                                       const int32_t* __restrict__ tail, const double* __restrict__ eps,
+                                       double* __restrict__ next, double* __restrict__ next_neg,
+                                       const double* __restrict__ eps_neg, int64_t ne, int64_t nv, int n_epochs,
+                                       double a, double b, double gamma, double initial_alpha, uint64_t seed) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  auto clip = [](double v) { return v > 4.0 ? 4.0 : (v < -4.0 ? -4.0 : v); };
+  double alpha = initial_alpha;
+  for (int n = 0; n < n_epochs; ++n) {
+    for (int64_t i = 0; i < ne; ++i) {
+      if (eps[i] <= 0.0 || next[i] > double(n)) continue;
+      const int64_t j = head[i], k = tail[i];
+      float* cur = y + j * dim;
+      float* oth = y + k * dim;
+      const double d2 = sq_dist64(cur, oth, dim);
+      double gc = 0.0;
+      if (d2 > 0.0) gc = -2.0 * a * b * pow(d2, b - 1.0) / (a * pow(d2, b) + 1.0);
+      for (int d = 0; d < dim; ++d) {
+        const double g = clip(__dmul_rn(gc, double(__fsub_rn(cur[d], oth[d]))));
+        cur[d] = float(__dadd_rn(double(cur[d]), __dmul_rn(g, alpha)));
+        oth[d] = float(__dadd_rn(double(oth[d]), __dmul_rn(-g, alpha)));
+      }
+      next[i] += eps[i];
+      const int nneg = int((double(n) - next_neg[i]) / eps_neg[i]);
+      for (int p = 0; p < nneg; ++p) {
+        const int64_t kk = neg_vertex(seed, n, i, p, nv);
+        const float* o = y + kk * dim;
+        const double e2 = sq_dist64(cur, o, dim);
+        double rc;
+        if (e2 > 0.0) rc = 2.0 * gamma * b / ((0.001 + e2) * (a * pow(e2, b) + 1.0));
+        else if (j == kk) continue;
+        else rc = 0.0;
+        for (int d = 0; d < dim; ++d) {
+          const double g = rc > 0.0 ? clip(__dmul_rn(rc, double(__fsub_rn(cur[d], o[d])))) : 4.0;
+          cur[d] = float(__dadd_rn(double(cur[d]), __dmul_rn(g, alpha)));
+        }
+      }
+      next_neg[i] += double(nneg) * eps_neg[i];
+    }
+    alpha = initial_alpha * (1.0 - double(n) / double(n_epochs));
   }
 }
 
 }  // namespace
 
-extern "C" int sg_umap_layout(sg_handle* h, const int32_t* head, const int32_t* tail, const float* epochs_per_sample,
-                              int64_t n_edges, int64_t n_vertices, int32_t dim, float* embedding, int32_t n_epochs,
-                              float a, float b, float gamma, float initial_alpha, float negative_sample_rate,
-                              uint64_t seed, void* stream) {
+extern "C" int sg_umap_layout(sg_handle* h, const int32_t* head, const int32_t* tail,
+                              const double* epochs_per_sample, int64_t n_edges, int64_t n_vertices, int32_t dim,
+                              float* embedding, int32_t n_epochs, float a, float b, float gamma, float initial_alpha,
+                              float negative_sample_rate, uint64_t seed, int32_t sequential, void* stream) {
   SG_HANDLE_CHECK(h);
   SG_ARG(head && tail && epochs_per_sample && embedding, "sg_umap_layout: null pointer argument");
   SG_ARG(n_edges >= 0 && n_vertices >= 1, "sg_umap_layout: bad sizes");
@@ -118,7 +182,7 @@ extern "C" int sg_umap_layout(sg_handle* h, const int32_t* head, const int32_t* 
   if (n_edges == 0) return SG_OK;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   void* buf = nullptr;
-  const size_t need = 3 * sg::Carver::need(sizeof(float) * size_t(n_edges));
+  const size_t need = 3 * sg::Carver::need(sizeof(double) * size_t(n_edges));
   SG_CUDA(cudaMallocAsync(&buf, need, st));
   struct Free {
     void* p;
@@ -126,13 +190,21 @@ extern "C" int sg_umap_layout(sg_handle* h, const int32_t* head, const int32_t* 
     ~Free() { cudaFreeAsync(p, s); }
   } guard{buf, st};
   sg::Carver cv(buf);
-  float* next = cv.take<float>(size_t(n_edges));
-  float* next_neg = cv.take<float>(size_t(n_edges));
-  float* eps_neg = cv.take<float>(size_t(n_edges));
+  double* next = cv.take<double>(size_t(n_edges));
+  double* next_neg = cv.take<double>(size_t(n_edges));
+  double* eps_neg = cv.take<double>(size_t(n_edges));
   sg::ProfScope prof(h, "umap_layout", st);
-  umap_init_kernel<<<sg::ceil_div_i(n_edges, 256), 256, 0, st>>>(epochs_per_sample, n_edges, negative_sample_rate,
-                                                                 next, next_neg, eps_neg);
+  umap_init_kernel<<<sg::ceil_div_i(n_edges, 256), 256, 0, st>>>(epochs_per_sample, n_edges,
+                                                                 double(negative_sample_rate), next, next_neg,
+                                                                 eps_neg);
   SG_LAUNCH_CHECK();
+  if (sequential) {
+    umap_sequential_kernel<<<1, 1, 0, st>>>(embedding, dim, head, tail, epochs_per_sample, next, next_neg, eps_neg,
+                                            n_edges, n_vertices, n_epochs, double(a), double(b), double(gamma),
+                                            double(initial_alpha), seed);
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+  }
   const unsigned grid = unsigned(std::min<int64_t>(sg::ceil_div(n_edges, 256), int64_t(h->sm_count) * 16));
   float alpha = initial_alpha;
   for (int n = 0; n < n_epochs; ++n) {

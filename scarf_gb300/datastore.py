@@ -11,6 +11,8 @@ the device (its float64 ``data`` dataset is written only when
 """
 from __future__ import annotations
 
+import os
+
 import logging
 from typing import Optional
 
@@ -183,6 +185,22 @@ class DataStore:
                                              self.z.require_group(assay_name), device)}
         setattr(self, assay_name, self._assays[assay_name])
         self._ann_cache = {}
+
+    @classmethod
+    def from_zarr(cls, store: str, assay_name: str = "RNA", precision: str = "plain", device="cuda",
+                  **kw) -> "DataStore":
+        """A DataStore over a scarf zarr directory store: the assay's count
+        chunks (``{assay}/counts``, Blosc-LZ4) decoded and turned into CSR on
+        the device, gene ids from ``{assay}/featureData/ids`` and cell ids
+        from ``cellData/ids`` when present (scarf/writers.py:58-89, :164-204)."""
+        from .zarr_io import read_counts_csr, read_strings
+        ip, ind, dat, n_genes = read_counts_csr(store, f"{assay_name}/counts", device=device)
+        gid = f"{assay_name}/featureData/ids"
+        genes = read_strings(store, gid, device) if os.path.exists(os.path.join(store, gid, ".zarray")) else None
+        cells = read_strings(store, "cellData/ids", device) \
+            if os.path.exists(os.path.join(store, "cellData", "ids", ".zarray")) else None
+        return cls(ip.cpu().numpy(), ind.cpu().numpy(), dat.cpu().numpy(), n_genes, gene_ids=genes, cell_ids=cells,
+                   assay_name=assay_name, precision=precision, device=device, **kw)
 
     def _get_assay(self, name: Optional[str]):
         return self._assays[name or self._defaultAssay]
@@ -505,7 +523,8 @@ def map_cells(ann_obj: AnnStream, indptr, indices, data, cmap: np.ndarray, missi
                         size_factor=size_factor, log_transform=norm_params["log_transform"],
                         renormalize_subset=norm_params["renormalize_subset"],
                         missing_mask=torch.from_numpy(missing).to(dev), fill_value=1.0)
-    s = K.project(x, ann_obj._mu32, ann_obj._sg32, ann_obj._l32, ann_obj.dims, n_cols=h)
+    s = K.project(x, ann_obj._mu32, ann_obj._sg32, ann_obj._l32, ann_obj.dims, n_cols=h,
+                  precision=ann_obj.annIdx.precision)
     idx, dist, _ = K.knn(s, ann_obj.annIdx.scores, ann_obj.dims, k, self_offset=-1,
                          margin=ann_obj.annIdx._margin(), precision=ann_obj.annIdx.precision)
     return idx.cpu().numpy(), dist.cpu().numpy()

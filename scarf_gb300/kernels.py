@@ -10,6 +10,7 @@ import ctypes as C
 import threading
 from typing import Optional, Tuple
 
+import numpy as np
 import torch
 
 from . import _lib as L
@@ -209,8 +210,9 @@ def filter_residual(device: Optional[int] = None) -> float:
 
 
 def project(x: torch.Tensor, mu32, sigma32, loadings32: torch.Tensor, d: int, n_cols: Optional[int] = None,
-            ld_s: Optional[int] = None, bf16_ld: Optional[int] = None):
-    """a5: scores = ((x - mu)/sigma) . L as float32 (n x ld_s), optionally a BF16 copy."""
+            ld_s: Optional[int] = None, bf16_ld: Optional[int] = None, precision: str = "plain"):
+    """a5: scores = ((x - mu)/sigma) . L as float32 (n x ld_s), optionally a BF16
+    copy; "plain" in FP32 SIMT, "precision" as 3xBF16 tcgen05 products."""
     _need(x, "x", torch.float32, 2, contiguous=False)
     _need(loadings32, "loadings32", torch.float32, 2)
     h = int(n_cols if n_cols is not None else mu32.numel())
@@ -222,7 +224,7 @@ def project(x: torch.Tensor, mu32, sigma32, loadings32: torch.Tensor, d: int, n_
         sb = torch.empty((x.shape[0], bf16_ld), dtype=torch.bfloat16, device=dev)
     L.check(L.load().sg_project(handle(dev.index).ptr, _p(x), x.shape[0], h, x.stride(0), _p(mu32), _p(sigma32),
                                 _p(loadings32), d, loadings32.stride(0), _p(scores), ld_s, _p(sb),
-                                bf16_ld or 0, _stream(dev)))
+                                bf16_ld or 0, PRECISIONS[precision], _stream(dev)))
     return (scores, sb) if bf16_ld else scores
 
 
@@ -310,19 +312,19 @@ def merge_graphs(indices, weights, snns):
 
 def umap_layout(head: torch.Tensor, tail: torch.Tensor, epochs_per_sample: torch.Tensor, embedding: torch.Tensor,
                 n_epochs: int, a: float, b: float, gamma: float = 1.0, initial_alpha: float = 1.0,
-                negative_sample_rate: float = 5.0, seed: int = 0) -> torch.Tensor:
+                negative_sample_rate: float = 5.0, seed: int = 0, sequential: bool = False) -> torch.Tensor:
     """f3: UMAP layout epochs on ``embedding`` (n x dim float32, in place; see
     sg_umap_layout). ``head``/``tail`` int32 edge endpoints, ``epochs_per_sample``
-    float32 per edge."""
+    float64 per edge; ``sequential`` runs the deterministic one-thread loop."""
     _need(head, "head", torch.int32, 1)
     _need(tail, "tail", torch.int32, 1)
-    _need(epochs_per_sample, "epochs_per_sample", torch.float32, 1)
+    _need(epochs_per_sample, "epochs_per_sample", torch.float64, 1)
     _need(embedding, "embedding", torch.float32, 2)
     dev = embedding.device
     L.check(L.load().sg_umap_layout(handle(dev.index).ptr, _p(head), _p(tail), _p(epochs_per_sample), head.numel(),
                                     embedding.shape[0], embedding.shape[1], _p(embedding), int(n_epochs), float(a),
                                     float(b), float(gamma), float(initial_alpha), float(negative_sample_rate),
-                                    C.c_uint64(int(seed) & ((1 << 64) - 1)), _stream(dev)))
+                                    C.c_uint64(int(seed) & ((1 << 64) - 1)), int(bool(sequential)), _stream(dev)))
     return embedding
 
 
@@ -365,3 +367,41 @@ def profile_query(name: str, device: Optional[int] = None) -> Tuple[float, int]:
     cnt = C.c_longlong()
     L.check(L.load().sg_profile_query(handle(device).ptr, name.encode(), C.byref(ms), C.byref(cnt)))
     return ms.value, cnt.value
+
+
+def blosc_decode(frames, out: torch.Tensor, out_starts) -> torch.Tensor:
+    """f2: decode Blosc1/LZ4 frames (a list of host ``bytes``) into the device
+    uint8 buffer ``out`` at the given byte offsets (see sg_blosc_decode)."""
+    _need(out, "out", torch.uint8, 1)
+    n = len(frames)
+    offs = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum([len(f) for f in frames], out=offs[1:])
+    buf = np.frombuffer(b"".join(frames), dtype=np.uint8) if n else np.zeros(1, np.uint8)
+    starts = np.ascontiguousarray(out_starts, dtype=np.int64)
+    if len(starts) != n:
+        raise ValueError("one output offset per frame")
+    dev = out.device
+    L.check(L.load().sg_blosc_decode(handle(dev.index).ptr, buf.ctypes.data_as(C.c_void_p),
+                                     offs.ctypes.data_as(C.c_void_p), n, _p(out), out.numel(),
+                                     starts.ctypes.data_as(C.c_void_p), _stream(dev)))
+    return out
+
+
+def chunks_to_csr(chunks: torch.Tensor, n_rows: int, chunk_rows: int, chunk_cols: int, n_cols: int,
+                  indptr_base: int = 0):
+    """f2: CSR (indptr int64, indices int32, data int32) of one band of decoded
+    dense uint32 chunks held as int32 in ``chunks`` (see sg_chunks_to_csr)."""
+    _need(chunks, "chunks", torch.int32, 1)
+    dev = chunks.device
+    h = handle(dev.index)
+    lib = L.load()
+    indptr = torch.empty(n_rows + 1, dtype=torch.int64, device=dev)
+    nnz = C.c_int64()
+    L.check(lib.sg_chunks_to_csr(h.ptr, _p(chunks), n_rows, chunk_rows, chunk_cols, n_cols, indptr_base,
+                                 _p(indptr), None, None, 0, C.byref(nnz), _stream(dev)))
+    cap = max(1, nnz.value)
+    ind = torch.empty(cap, dtype=torch.int32, device=dev)
+    dat = torch.empty(cap, dtype=torch.int32, device=dev)
+    L.check(lib.sg_chunks_to_csr(h.ptr, _p(chunks), n_rows, chunk_rows, chunk_cols, n_cols, indptr_base,
+                                 _p(indptr), _p(ind), _p(dat), cap, C.byref(nnz), _stream(dev)))
+    return indptr, ind[:nnz.value], dat[:nnz.value]

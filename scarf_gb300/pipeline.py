@@ -176,7 +176,7 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k:
     if eigh is None:
         eigh = "filter" if precision == "precision" else "fp64"
     comps, evals, evr, l32 = K.pca_basis(cov, zsum, n_used, dims + 1, n_load=dims, ld_l=dims, eigh=eigh)
-    scores = K.project(x, mu32, sigma32, l32, dims, n_cols=h)
+    scores = K.project(x, mu32, sigma32, l32, dims, n_cols=h, precision=precision)
     if margin is None:
         margin = PRECISION_MARGIN if precision == "precision" else PLAIN_MARGIN
     K.set_autotune(autotune, dev.index)

@@ -409,7 +409,7 @@ class MappingServer:
         x = K.normalize_csr(t_ip, t_ind[off:], t_dat[off:], self.cmap, h, size_factor=self.size_factor,
                             log_transform=self.log_transform, renormalize_subset=self.renorm,
                             missing_mask=self.missing, fill_value=1.0)
-        s = K.project(x, ref._mu32, ref._sg32, ref._l32, ref.dims, n_cols=h)
+        s = K.project(x, ref._mu32, ref._sg32, ref._l32, ref.dims, n_cols=h, precision=self.precision)
         return K.knn(s, ref.annIdx.scores, ref.dims, self.k, self_offset=-1, margin=ref.annIdx._margin(),
                      precision=self.precision)
 

@@ -69,7 +69,7 @@ def simplicial_set_embedding(g, embedding, n_epochs, a, b, random_seed, gamma, i
     rows, cols, w = g
     eps = make_epochs_per_sample(w.cpu().numpy(), n_epochs)
     y = torch.from_numpy(np.ascontiguousarray(embedding, dtype=np.float32)).cuda()
-    K.umap_layout(rows, cols, torch.from_numpy(eps.astype(np.float32)).cuda(), y, n_epochs, a, b, gamma,
+    K.umap_layout(rows, cols, torch.from_numpy(eps.astype(np.float64)).cuda(), y, n_epochs, a, b, gamma,
                   initial_alpha, negative_sample_rate, seed=int(random_seed))
     return y.cpu().numpy()
 

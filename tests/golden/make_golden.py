@@ -12,6 +12,8 @@ Two kinds of fixtures are written:
   re-saved compressed. ``knn_weights`` is a known answer for the smoothing
   step given the indices and distances (one chunk of 808 rows, k=11,
   lc=1.0, bw=1.5).
+* ``zarr_chunks.npz`` -- Blosc-LZ4 chunks of the reference's test store and
+  the cell totals that pin their decoding (see ``zarr_chunks``).
 * ``ref_functions.npz`` -- seeded small inputs and the outputs of the
   reference's own functions, executed from its source files. scarf's package
   import pulls dask/zarr/numba, which are absent, so each function is lifted
@@ -98,9 +100,64 @@ class _ExactIndex:
         return i.astype(np.uint64), d.astype(np.float32)
 
 
+def zarr_chunks(ds: Path):
+    """``zarr_chunks.npz``: Blosc-LZ4 chunks of the reference's own test store
+    (``1K_pbmc_citeseq.zarr.tar.gz``, written by scarf's create_zarr_dataset,
+    scarf/writers.py:58-89): the first and last RNA count chunks (bit shuffle,
+    split streams, a ragged last block), the one ADT count chunk and the cell
+    ids (byte shuffle). The oracle's decoder is pinned here on the whole RNA
+    matrix: its per-cell totals and non-zero counts must equal the reference's
+    ``RNA_nCounts`` / ``RNA_nFeatures`` in ``cell_attributes.csv`` for every
+    listed cell (and ``assay2_*`` for the ADT chunk)."""
+    import csv
+    import hashlib
+    import json
+    import tarfile
+    import tempfile
+    from oracle import blosc
+    with tempfile.TemporaryDirectory() as tmp:
+        with tarfile.open(ds / "1K_pbmc_citeseq.zarr.tar.gz") as tf:
+            tf.extractall(tmp, filter="data")
+        root = Path(tmp)
+        rna_meta = json.loads((root / "RNA" / "counts" / ".zarray").read_text())
+        adt_meta = json.loads((root / "assay2" / "counts" / ".zarray").read_text())
+        ids_meta = json.loads((root / "cellData" / "ids" / ".zarray").read_text())
+        n_cells, n_genes = rna_meta["shape"]
+        cr, cc = rna_meta["chunks"]
+        nchunk = -(-n_genes // cc)
+        frames = {f"rna_0_{c}": (root / "RNA" / "counts" / f"0.{c}").read_bytes() for c in (0, nchunk - 1)}
+        frames["adt_0_0"] = (root / "assay2" / "counts" / "0.0").read_bytes()
+        frames["cell_ids_0"] = (root / "cellData" / "ids" / "0").read_bytes()
+        ids = np.frombuffer(blosc.decompress(frames["cell_ids_0"]), dtype=ids_meta["dtype"])[:n_cells]
+        tot = np.zeros(n_cells, np.int64)
+        nz = np.zeros(n_cells, np.int64)
+        for c in range(nchunk):
+            b = blosc.decode_chunk((root / "RNA" / "counts" / f"0.{c}").read_bytes(), (cr, cc), "<u4")[:n_cells]
+            w = min(cc, n_genes - c * cc)
+            tot += b[:, :w].sum(1, dtype=np.int64)
+            nz += (b[:, :w] > 0).sum(1)
+        adt = blosc.decode_chunk(frames["adt_0_0"], tuple(adt_meta["chunks"]), "<u4")[:n_cells, :adt_meta["shape"][1]]
+    rows = list(csv.DictReader(open(ds / "cell_attributes.csv")))
+    pos = {v: i for i, v in enumerate(ids)}
+    sel = np.array([pos[r["ids"]] for r in rows])
+    col = lambda k: np.array([float(r[k]) for r in rows])  # noqa: E731
+    assert np.array_equal(tot[sel], col("RNA_nCounts")) and np.array_equal(nz[sel], col("RNA_nFeatures"))
+    assert np.array_equal(adt.sum(1)[sel], col("assay2_nCounts"))
+    assert np.array_equal((adt > 0).sum(1)[sel], col("assay2_nFeatures"))
+    out = {k: np.frombuffer(v, dtype=np.uint8) for k, v in frames.items()}
+    out.update({f"sha256_{k}": np.array(hashlib.sha256(blosc.decompress(v)).hexdigest()) for k, v in frames.items()})
+    out.update(rna_zarray=np.array(json.dumps(rna_meta)), adt_zarray=np.array(json.dumps(adt_meta)),
+               ids_zarray=np.array(json.dumps(ids_meta)), csv_ids=np.array([r["ids"] for r in rows]),
+               csv_rna_ncounts=col("RNA_nCounts"), csv_rna_nfeatures=col("RNA_nFeatures"),
+               csv_adt_ncounts=col("assay2_nCounts"), csv_adt_nfeatures=col("assay2_nFeatures"),
+               rna_totals_all_chunks=tot, rna_nnz_all_chunks=nz, rna_last_chunk=np.int64(nchunk - 1))
+    np.savez_compressed(HERE / "zarr_chunks.npz", **out)
+
+
 def main(ref_root: str):
     ref = Path(ref_root) / "scarf"
     ds = ref / "tests" / "datasets"
+    zarr_chunks(ds)
     np.savez_compressed(
         HERE / "pbmc1k_knn.npz",
         indices=np.load(ds / "knn_indices.npy"),

@@ -86,3 +86,100 @@ def multirank_worker(rank, ws, port, q):
     q.put((rank, bench.max_over_ranks(10.0 + rank, torch.device("cpu")), bench.dist_env()))
     dist.barrier()
     dist.destroy_process_group()
+
+
+# ---- Blosc1 / LZ4 / bit-shuffle frames for decoder tests (the encoder side of
+# the published formats, small and simple: greedy LZ4 matching, no search) ----
+def lz4_compress(data: bytes, min_match: int = 4) -> bytes:
+    """A valid LZ4 block of ``data``: greedy matches found through a table of
+    the last position of each 4-byte prefix (offsets < 65536, overlapping
+    matches allowed), the last 5 bytes as literals as the format requires."""
+    out = bytearray()
+    n = len(data)
+    table = {}
+    i = anchor = 0
+
+    def length_bytes(v):
+        while v >= 255:
+            out.append(255)
+            v -= 255
+        out.append(v)
+
+    def emit(lit_start, lit_end, off=None, mlen=0):
+        lit = lit_end - lit_start
+        tok_l = min(lit, 15)
+        tok_m = 0 if off is None else min(mlen - 4, 15)
+        out.append((tok_l << 4) | tok_m)
+        if lit >= 15:
+            length_bytes(lit - 15)
+        out.extend(data[lit_start:lit_end])
+        if off is not None:
+            out.extend((off & 255, off >> 8))
+            if mlen - 4 >= 15:
+                length_bytes(mlen - 4 - 15)
+
+    while i + 12 <= n:
+        key = data[i:i + 4]
+        j = table.get(key)
+        table[key] = i
+        if j is not None and i - j < 65536:
+            m = 4
+            while i + m < n - 5 and data[j + m] == data[i + m]:
+                m += 1
+            if m >= min_match:
+                emit(anchor, i, i - j, m)
+                i += m
+                anchor = i
+                continue
+        i += 1
+    emit(anchor, n)
+    return bytes(out)
+
+
+def bitshuffle(buf: bytes, typesize: int) -> bytes:
+    n = len(buf) // typesize
+    n8 = n - n % 8
+    if n8 == 0:
+        return bytes(buf)
+    e = np.frombuffer(buf[:n8 * typesize], dtype=np.uint8).reshape(n8, typesize)
+    bits = np.unpackbits(e, axis=1, bitorder="little").reshape(n8, typesize, 8)   # [e, b, j]
+    planes = bits.transpose(1, 2, 0).reshape(typesize * 8, n8)                   # [8 b + j, e]
+    return np.packbits(planes, axis=1, bitorder="little").tobytes() + bytes(buf[n8 * typesize:])
+
+
+def byteshuffle(buf: bytes, typesize: int) -> bytes:
+    n = len(buf) // typesize
+    body = np.frombuffer(buf[:n * typesize], dtype=np.uint8).reshape(n, typesize).T.reshape(-1)
+    return body.tobytes() + bytes(buf[n * typesize:])
+
+
+def blosc_frame(data: bytes, typesize: int, blocksize: int, shuffle: str = "bit", split: bool = True,
+                raw_streams: bool = False, memcpy: bool = False) -> bytes:
+    """A Blosc1 frame (LZ4 codec) of ``data`` in the layout c-blosc 1.x writes."""
+    import struct
+    flags = (1 << 5) | {"bit": 0x04, "byte": 0x01, "none": 0}[shuffle] | (0 if split else 0x10)
+    nbytes = len(data)
+    if memcpy:
+        hdr = struct.pack("<BBBBIII", 2, 1, flags | 0x02, typesize, nbytes, blocksize, 16 + nbytes)
+        return hdr + data
+    nblocks = -(-nbytes // blocksize)
+    body = bytearray()
+    starts = []
+    base = 16 + 4 * nblocks
+    for b in range(nblocks):
+        blk = data[b * blocksize:(b + 1) * blocksize]
+        if shuffle == "bit":
+            blk = bitshuffle(blk, typesize)
+        elif shuffle == "byte":
+            blk = byteshuffle(blk, typesize)
+        ns = typesize if (split and len(blk) == blocksize) else 1
+        starts.append(base + len(body))
+        sl = len(blk) // ns
+        for k in range(ns):
+            s = blk[k * sl:(k + 1) * sl]
+            c = s if raw_streams else lz4_compress(s)
+            if len(c) >= len(s):
+                c = s          # stored raw: the compressed size equals the stream's length
+            body += struct.pack("<i", len(c)) + c
+    hdr = struct.pack("<BBBBIII", 2, 1, flags, typesize, nbytes, blocksize, base + len(body))
+    return hdr + struct.pack(f"<{nblocks}i", *starts) + bytes(body)

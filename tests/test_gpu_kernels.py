@@ -262,30 +262,36 @@ def test_pca_basis_and_projection(K, counts):
     assert torch.all(scores[:, dims:] == 0)
 
 
-def test_projection_gemm_path(K):
-    """From 4,096 rows the projection is one tensor-core GEMM over the
-    uncentred rows with the centring folded into a per-column shift; it agrees
-    with the oracle's reducer on the same basis, pads with zeros and writes
-    the optional BF16 copy."""
-    indptr, indices, data, G, _ = small_counts(n_cells=6000, seed=3)
+@pytest.mark.parametrize("form,n_cells,dims,ld_s,bf16_ld", [("plain", 6000, 30, 32, 40),
+                                                          ("precision", 6000, 30, 32, 40),
+                                                          ("precision", 1000, 50, 52, 72),
+                                                          ("precision", 131, 7, 8, 0)])
+def test_projection_forms(K, form, n_cells, dims, ld_s, bf16_ld):
+    """The reducer in both forms against the oracle's on the same basis: the
+    plain form in FP32 SIMT, the precision form as 3xBF16 tcgen05 products of
+    the uncentred rows with the centring as a per-column shift (several
+    tiles, a ragged last tile and feature chunk, d up to 50). Both pad with
+    zeros and write the optional BF16 copy."""
+    indptr, indices, data, G, _ = small_counts(n_cells=n_cells, seed=3)
     feat = top_var_genes(indptr, indices, data, G, 300)
     counts = (indptr, indices, data, G, feat)
     x, cs, cq, _ = _normalize(K, counts)
     mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
     xw, omu, osg, z = _zscaled(counts)
     h = z.shape[1]
-    dims = 30
     cov, zsum = K.covariance(x, mu32, sg32, n_cols=h)
     comps, _, _, l32 = K.pca_basis(cov, zsum, x.shape[0], dims + 1, n_load=dims, ld_l=dims)
-    assert x.shape[0] >= 4096
-    scores, sb = K.project(x, mu32, sg32, l32, dims, n_cols=h, ld_s=32, bf16_ld=40)
+    out = K.project(x, mu32, sg32, l32, dims, n_cols=h, ld_s=ld_s, bf16_ld=bf16_ld, precision=form)
+    scores, sb = out if bf16_ld else (out, None)
     torch.cuda.synchronize()
     want = oracle.reducer(xw, omu, osg, comps.cpu().numpy()[:, :dims])
     got = scores[:, :dims].cpu().numpy()
-    assert np.abs(got - want).max() <= 1e-4 * max(1.0, np.abs(want).max())
+    tol = 2e-5 if form == "plain" else 1e-4
+    assert np.abs(got - want).max() <= tol * max(1.0, np.abs(want).max())
     assert torch.all(scores[:, dims:] == 0)
-    assert torch.all(sb[:, dims:].float() == 0)
-    assert torch.equal(sb[:, :dims], scores[:, :dims].to(torch.bfloat16))
+    if sb is not None:
+        assert torch.all(sb[:, dims:].float() == 0)
+        assert torch.equal(sb[:, :dims], scores[:, :dims].to(torch.bfloat16))
 
 
 def _self_knn(K, pts, k, **kw):
@@ -343,6 +349,23 @@ def test_knn_plain_and_precision_agree(K):
     b = _self_knn(K, pts, 21, precision="precision", margin=16)
     same = (a[0] == b[0]).mean()
     assert same >= 0.99
+
+
+def test_self_knn_precision_locality_order(K):
+    # From 32,768 rows the precision self-kNN sorts the rows by their nearest
+    # pilot row and starts each CTA's reference scan at its own tile; the
+    # neighbours must be those of the exact FP32 plain form all the same.
+    n, d, k = 40000, 50, 21
+    pts = clustered_points(n, d, n_clusters=20, seed=77, dup=((5, 6), (10, 11), (10, 12), (30000, 39999)))
+    pi, pd, pm = _self_knn(K, pts, k)
+    gi, gd, gm = _self_knn(K, pts, k, precision="precision", margin=16)
+    assert gm == pm
+    assert (gi == pi).mean() >= 0.999
+    assert np.abs(gd - pd).max() <= 1e-5 * max(1.0, pd.max())
+    rows = np.random.default_rng(0).choice(n, 1500, replace=False)
+    _, ed = oracle.exact_knn(pts[rows], pts, k + 1)
+    # the k+1-th exact distance bounds the k kept after the self hit is dropped
+    assert oracle.recall_at_k(pts[rows], pts, gi[rows], ed[:, -1]) >= 0.995
 
 
 def test_knn_query_mapping(K):
@@ -558,7 +581,7 @@ def test_umap_layout_matches_sequential_restatement_in_quality(K):
     eps = oracle.umap_make_epochs_per_sample(w, 60)
     y0 = (np.random.default_rng(1).normal(size=(400, 2)) * 10).astype(np.float32)
     y = cu(y0.copy())
-    K.umap_layout(cu(head.astype(np.int32)), cu(tail.astype(np.int32)), cu(eps.astype(np.float32)), y, 60, a, b,
+    K.umap_layout(cu(head.astype(np.int32)), cu(tail.astype(np.int32)), cu(eps.astype(np.float64)), y, 60, a, b,
                   seed=3)
     torch.cuda.synchronize()
     got = y.cpu().numpy()
@@ -570,6 +593,34 @@ def test_umap_layout_matches_sequential_restatement_in_quality(K):
     assert embedding_purity(y0, lab) < 0.5
     assert pw > 0.95 and pg > 0.85
     assert pg >= pw - 0.1
+
+
+@pytest.mark.gpu
+def test_umap_layout_sequential_mode_pins_the_restatement(K):
+    """The deterministic mode of sg_umap_layout (one thread, edges in order,
+    umap-learn's float64 gradient arithmetic on float32 coordinates and its
+    float64 sampling schedule) follows the oracle's restatement of
+    optimize_layout_euclidean step for step when both draw the same negative
+    samples (the kernel's counter hash, restated in the oracle): the same
+    trajectory to float32 rounding after 40 epochs on a 300-point graph."""
+    from helpers import umap_graph
+    x, lab, _, head, tail, w = umap_graph(300, 10, 4, 10, seed=9)
+    a, b = (float(np.float32(v)) for v in oracle.umap_find_ab_params(1.0, 0.1))
+    eps = oracle.umap_make_epochs_per_sample(w, 40)
+    y0 = (np.random.default_rng(4).normal(size=(300, 2)) * 10).astype(np.float32)
+    seed = 12345
+    y = cu(y0.copy())
+    K.umap_layout(cu(head.astype(np.int32)), cu(tail.astype(np.int32)), cu(eps.astype(np.float64)), y, 40, a, b,
+                  seed=seed, sequential=True)
+    torch.cuda.synchronize()
+    got = y.cpu().numpy()
+    want = oracle.umap_layout_sequential(y0, head, tail, eps, 40, a, b,
+                                         rand_vertex=lambda n, i, p: oracle.umap_negative_vertex(seed, n, i, p, 300))
+    assert np.isfinite(got).all()
+    err = np.abs(got - want).max()
+    assert err <= 1e-3 * max(1.0, np.abs(want).max()), f"sequential layout differs by {err}"
+    # most coordinates agree bit for bit (the two pow implementations may round differently)
+    assert np.mean(got == want) > 0.9
 
 
 @pytest.mark.gpu
