@@ -67,13 +67,19 @@ int sg_profile(sg_handle* h, int enable);
 
 /* Autotuning (no reference counterpart): with enable != 0, the first
  * precision-form sg_knn of a shape bucket (log2 of the query rows, log2 of the
- * reference rows, d, candidate-list length) with at least 1e9 query-reference
- * pairs times three reference split counts and keeps the fastest for later
+ * reference rows, d, candidate-list length, self-kNN or not) with at least
+ * 1e9 query-reference pairs times three reference split counts (each with and
+ * without the locality order for a self-kNN) and keeps the fastest for later
  * calls of that bucket on this handle. Off by default: the first call of a
- * bucket then costs about three calls. sg_knn_last_splits returns the split
+ * bucket then costs three to six calls. sg_knn_last_splits returns the split
  * count of the last precision-form sg_knn. */
 int sg_set_autotune(sg_handle* h, int enable);
 int sg_knn_last_splits(const sg_handle* h);
+/* 1 when the last precision-form sg_knn on the handle ran its self-kNN in the
+ * locality order (rows sorted by their nearest pilot row, each CTA starting
+ * its reference scan at its own rows), else 0. The autotuner times a
+ * self-kNN with and without it. */
+int sg_knn_last_locality(const sg_handle* h);
 int sg_profile_reset(sg_handle* h);
 
 /* Bounded-wait test hooks (no reference counterpart). Every mbarrier wait of

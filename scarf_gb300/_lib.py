@@ -57,6 +57,7 @@ SIGNATURES = {
     "sg_pca_filter_residual": (C.c_double, [vp]),
     "sg_set_autotune": (C.c_int, [vp, C.c_int]),
     "sg_knn_last_splits": (C.c_int, [vp]),
+    "sg_knn_last_locality": (C.c_int, [vp]),
     "sg_set_wait_limit": (C.c_int, [vp, u32]),
     "sg_test_idle_mma": (C.c_int, [vp]),
     "sg_project": (C.c_int, [vp, vp, i64, i32, i64, vp, vp, vp, i32, i32, vp, i32, vp, i32, i32, vp]),

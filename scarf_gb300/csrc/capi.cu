@@ -139,6 +139,8 @@ int sg_set_autotune(sg_handle* h, int enable) {
 
 int sg_knn_last_splits(const sg_handle* h) { return h ? h->last_knn_splits : 0; }
 
+int sg_knn_last_locality(const sg_handle* h) { return h ? h->last_knn_locality : 0; }
+
 int sg_set_wait_limit(sg_handle* h, uint32_t polls) {
   if (!h) return sg::fail(SG_ERR_ARG, "null sg_handle");
   h->wait_limit = polls;

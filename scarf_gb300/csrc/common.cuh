@@ -29,10 +29,12 @@ struct sg_handle {
   // count per (log2 query rows, log2 reference rows, d, list length) bucket
   bool autotune = false;
   struct KnnTune {
-    int qb, rb, d, kc, nsplit;
+    int qb, rb, d, kc, nsplit, loc;
+    bool self;
   };
   std::vector<KnnTune> knn_tune;
   int last_knn_splits = 0;
+  int last_knn_locality = 0;
   // bounded-wait test hooks (sg_set_wait_limit, sg_test_idle_mma): the poll
   // limit of the tensor-core kernels' mbarrier waits (0 = the default), and a
   // one-shot switch that keeps the next precision kNN's MMA issuer idle

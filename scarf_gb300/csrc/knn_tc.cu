@@ -513,6 +513,10 @@ __global__ void bin_scatter_kernel(const int* __restrict__ pid, int64_t n, int n
   }
 }
 
+__global__ void add_count_kernel(unsigned long long* __restrict__ dst, const unsigned long long* __restrict__ src) {
+  *dst += *src;
+}
+
 // pilots used for n rows (0: no locality order)
 int pilots_for(int64_t n) {
   if (n < (int64_t(1) << 15)) return 0;
@@ -581,13 +585,18 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
     return r;
   };
   const int qb = ilog2(nq_pad), rb = ilog2(nr_pad);
-  int tuned = 0;
+  // self-kNN (the queries are the references): the rows can be put in a
+  // locality order (see pilots_for); the autotuner decides whether it pays
+  const int np_self = (queries == refs && nq == nr && self_offset == 0) ? pilots_for(nr) : 0;
+  int tuned = 0, tuned_loc = 1;
   for (const auto& e : h->knn_tune)
-    if (e.qb == qb && e.rb == rb && e.d == d && e.kc == kc) tuned = e.nsplit;
-  // self-kNN (the queries are the references): locality order of the rows
-  const int np = (queries == refs && nq == nr && self_offset == 0) ? pilots_for(nr) : 0;
+    if (e.qb == qb && e.rb == rb && e.d == d && e.kc == kc && e.self == (np_self > 0)) {
+      tuned = e.nsplit;
+      tuned_loc = e.loc;
+    }
+  auto run = [&](int nsplit, int loc, unsigned long long* miss) -> int {
+  const int np = loc ? np_self : 0;
   const int nblk = np ? sg::ceil_div_i(nr, kSortRows) : 0;
-  auto run = [&](int nsplit) -> int {
   const int64_t rps = sg::ceil_div(sg::ceil_div(nr, nsplit), BN) * BN;
   const int fold = d <= BK - 3 ? 1 : 0;
   const size_t need = sg::Carver::need(size_t(nr_pad) * BK * 2) + sg::Carver::need(size_t(nr_pad) * 4) +
@@ -645,27 +654,41 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   if (herr) return sg::fail(SG_ERR_TIMEOUT, "sg_knn: a tensor-core pipeline wait expired (stage %d)", herr);
   sg::ProfScope prof(h, "rerank", st);
   h->last_knn_splits = nsplit;
+  h->last_knn_locality = np > 0 ? 1 : 0;
   return sg_rerank(queries, refs, d, ld, nq, cand, nsplit, kc, nq_pad, kq, k, self_offset, idx_out, dist_out,
-                   nmiss, st);
+                   miss, st);
   };
-  if (tuned) return run(tuned);
-  if (!h->autotune || double(nq) * double(nr) < 1e9) return run(ns0);
-  // Autotune the split count for this (query, reference, d, list) bucket:
-  // time the heuristic, half and double of it (kernel + re-rank) once and keep
-  // the fastest. Every candidate returns the same exact top k; the last run's
-  // outputs stand.
-  std::vector<int> cands{ns0};
-  for (int c : {splits_for(std::max(1, ns0 / 2)), splits_for(ns0 * 2)})
-    if (std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
+  if (tuned) return run(tuned, tuned_loc, nmiss);
+  if (!h->autotune || double(nq) * double(nr) < 1e9) return run(ns0, 1, nmiss);
+  // Autotune the (split count, locality order) pair for this (query rows,
+  // reference rows, d, list length, self) bucket: time the heuristic split
+  // count, half and double of it, each with and without the locality order
+  // for a self-kNN (kernel + re-rank), once, and keep the fastest. Every
+  // candidate returns the same exact top k, so the last run's outputs stand;
+  // its miss count alone is added to n_missed.
+  struct Cand {
+    int ns, loc;
+  };
+  std::vector<Cand> cands;
+  for (int c : {ns0, splits_for(std::max(1, ns0 / 2)), splits_for(ns0 * 2)})
+    for (int loc : {1, 0}) {
+      if (loc == 0 && np_self == 0) continue;
+      bool dup = false;
+      for (const Cand& e : cands) dup |= (e.ns == c && e.loc == (np_self ? loc : 1));
+      if (!dup) cands.push_back({c, np_self ? loc : 1});
+    }
   cudaEvent_t e0, e1;
   SG_CUDA(cudaEventCreate(&e0));
   SG_CUDA(cudaEventCreate(&e1));
-  int best = ns0;
+  unsigned long long* trial_miss = nullptr;
+  if (nmiss) SG_CUDA(cudaMallocAsync(&trial_miss, sizeof(unsigned long long), st));
+  Cand best = cands[0];
   float best_ms = INFINITY;
   int rc = SG_OK;
-  for (int c : cands) {
+  for (const Cand& c : cands) {
+    if (trial_miss) SG_CUDA(cudaMemsetAsync(trial_miss, 0, sizeof(unsigned long long), st));
     SG_CUDA(cudaEventRecord(e0, st));
-    rc = run(c);
+    rc = run(c.ns, c.loc, trial_miss);
     if (rc) break;
     SG_CUDA(cudaEventRecord(e1, st));
     SG_CUDA(cudaEventSynchronize(e1));
@@ -676,9 +699,14 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
       best = c;
     }
   }
+  if (rc == SG_OK && trial_miss) {
+    add_count_kernel<<<1, 1, 0, st>>>(nmiss, trial_miss);
+    SG_LAUNCH_CHECK();
+  }
+  if (trial_miss) cudaFreeAsync(trial_miss, st);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc) return rc;
-  h->knn_tune.push_back({qb, rb, d, kc, best});
+  h->knn_tune.push_back({qb, rb, d, kc, best.ns, best.loc, np_self > 0});
   return SG_OK;
 }

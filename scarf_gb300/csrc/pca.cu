@@ -25,6 +25,7 @@
 #endif
 #include <vector>
 
+bool sg_project_tc_supported(const float* x, int64_t ld, int d);  // proj_tc.cu
 int sg_project_tc(sg_handle* h, const float* x, int64_t n_rows, int32_t n_cols, int64_t ld, const float* mu32,
                   const float* sigma32, const float* loadings32, int32_t d, int32_t ld_l, float* scores, int32_t ld_s,
                   __nv_bfloat16* sb, int32_t ld_b, cudaStream_t st);  // proj_tc.cu
@@ -1179,9 +1180,12 @@ extern "C" int sg_project(sg_handle* h, const float* x, int64_t n_rows, int32_t 
   SG_ARG(!bf16_out || ld_b >= d, "sg_project: ld_b < d");
   SG_ARG(precision == SG_PLAIN || precision == SG_PRECISION, "sg_project: unknown precision %d", precision);
   if (n_rows == 0) return SG_OK;
-  if (precision == SG_PRECISION)
+  // the precision form on the tensor cores; rows of x that TMA cannot address
+  // (an unaligned base or row stride) take the FP32 SIMT kernel instead
+  if (precision == SG_PRECISION && sg_project_tc_supported(x, ld, d))
     return sg_project_tc(h, x, n_rows, n_cols, ld, mu32, sigma32, loadings32, d, ld_l, scores, ld_s,
                          static_cast<__nv_bfloat16*>(bf16_out), ld_b, st);
+  SG_ARG(precision == SG_PLAIN || d <= 64, "sg_project: the precision form supports d <= 64");
   const int ccols = std::max<int>(ld_s, bf16_out ? ld_b : 0);
   sg::ProfScope prof(h, "project", st);
   dim3 grid(sg::ceil_div_i(n_rows, PR), sg::ceil_div_i(std::min<int>(ccols, sg::ceil_div_i(d, PC) * PC), PC));

@@ -202,6 +202,10 @@ def knn_last_splits(device: Optional[int] = None) -> int:
     return int(L.load().sg_knn_last_splits(handle(device).ptr))
 
 
+def knn_last_locality(device: Optional[int] = None) -> int:
+    return int(L.load().sg_knn_last_locality(handle(device).ptr))
+
+
 def filter_residual(device: Optional[int] = None) -> float:
     """Max relative FP64 residual of the wanted pairs of the last
     ``pca_basis(eigh='filter')`` on this thread's handle (NaN: dense route for

@@ -110,34 +110,52 @@ def normalize_csr_host(indptr, indices, data, n_genes: int, feat_idx, *, size_fa
     side = torch.cuda.Stream(dev)
     ipn = ip_h.numpy() if ip_h.device.type == "cpu" else ip_h.cpu().numpy()
     bounds = list(range(0, n, chunk_cells)) + [n]
-    staged = []
+    nch = len(bounds) - 1
+    # a ring of three device staging slots sized for the largest chunk: the
+    # copy of chunk i+1 (side stream) overlaps the normalisation of chunk i,
+    # and a slot is refilled only after the normalisation that read it is done
+    nnz_max = max(int(ipn[bounds[i + 1]] - ipn[bounds[i]]) for i in range(nch))
+    rows_max = max(bounds[i + 1] - bounds[i] for i in range(nch))
+    nslot = min(3, nch)
+    slots = [(torch.empty(rows_max + 1, dtype=torch.int64, device=dev),
+              torch.empty(max(1, nnz_max), dtype=torch.int32, device=dev),
+              torch.empty(max(1, nnz_max), dtype=torch.int32, device=dev)) for _ in range(nslot)]
+    freed = [None] * nslot          # event: the last normalisation that read the slot has finished
+    landed = [None] * nch
 
     def stage(ci):
         a, b = bounds[ci], bounds[ci + 1]
         pa, pb = int(ipn[a]), int(ipn[b])
+        sl = ci % nslot
+        t_ip, t_ind, t_dat = slots[sl]
         with torch.cuda.stream(side):
-            t_ip = ip_h[a:b + 1].to(dev, non_blocking=True)
-            t_ind = ind_h[pa:pb].to(dev, non_blocking=True)
-            t_dat = dat_h[pa:pb].to(dev, non_blocking=True)
+            if freed[sl] is not None:
+                side.wait_event(freed[sl])
+            t_ip[:b - a + 1].copy_(ip_h[a:b + 1], non_blocking=True)
+            t_ind[:pb - pa].copy_(ind_h[pa:pb], non_blocking=True)
+            t_dat[:pb - pa].copy_(dat_h[pa:pb], non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(side)
-        return a, b, t_ip, t_ind, t_dat, ev
+        landed[ci] = ev
 
-    nxt = stage(0)
-    for ci in range(len(bounds) - 1):
-        a, b, t_ip, t_ind, t_dat, ev = nxt
-        comp.wait_event(ev)
-        if ci + 2 < len(bounds):
-            nxt = stage(ci + 1)
-        K.normalize_csr(t_ip, t_ind, t_dat, cmap, h, size_factor=size_factor, log_transform=log_transform,
+    for ci in range(min(nslot, nch)):
+        stage(ci)
+    for ci in range(nch):
+        a, b = bounds[ci], bounds[ci + 1]
+        pa, pb = int(ipn[a]), int(ipn[b])
+        sl = ci % nslot
+        t_ip, t_ind, t_dat = slots[sl]
+        comp.wait_event(landed[ci])
+        K.normalize_csr(t_ip[:b - a + 1], t_ind[:max(1, pb - pa)], t_dat[:max(1, pb - pa)], cmap, h,
+                        size_factor=size_factor, log_transform=log_transform,
                         renormalize_subset=renormalize_subset,
                         n_counts=None if nc is None else nc[a:b], missing_mask=mm, fill_value=fill_value,
                         out=x[a:b], colsum=cs, colsumsq=cq)
-        for t in (t_ip, t_ind, t_dat):
-            t.record_stream(comp)
-        staged.append((t_ip, t_ind, t_dat))
-        if len(staged) > 2:
-            staged.pop(0)
+        done = torch.cuda.Event()
+        done.record(comp)
+        freed[sl] = done
+        if ci + nslot < nch:
+            stage(ci + nslot)
     return x, cs, cq
 
 
