@@ -448,6 +448,7 @@ def run_gb300(args, cfg):
     sampler.start()
     ms, res, launches, prof_ms, _ = timed("precision", args.steps, args.warmup, prof=True)
     clocks = sampler.stop()
+    knn_layout = {"splits": K.knn_last_splits(), "locality_order": bool(K.knn_last_locality())}
     rec, werr = graph_check(res, BATCH)
     ann_recall = res.recall()
     e2e_ms, res_h, _, _, outs = timed("precision", args.steps, args.warmup, host=True)
@@ -552,6 +553,7 @@ def run_gb300(args, cfg):
                   "vs_fp64_pipeline": truth["plain"], "speedup_precision_vs_plain": round(plain_ms / ms, 3),
                   "kernels_ms": {k_: round(v[0], 4) for k_, v in prof_p.items()}},
         "kernels": kernels,
+        "knn_layout": knn_layout,
         "eigh_parts": eig_parts,
         "eigensolver": eig,
         "kmeans": kmeans_info,
