@@ -741,6 +741,8 @@ def main():
     ap.add_argument("--form", default="precision", choices=["precision", "plain"], help="form used by --mode step")
     ap.add_argument("--knn-queries", type=int, default=110_000, help="--mode knn: query rows")
     ap.add_argument("--knn-refs", type=int, default=1_000_000, help="--mode knn: reference rows")
+    ap.add_argument("--knn-source", default=None, choices=sorted(CONFIGS),
+                    help="--mode knn: self-kNN of this config's PCA scores instead of clustered points")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup) if args.impl == "gb300" else args.warmup
     cfg = CONFIGS[args.config]
@@ -906,14 +908,51 @@ def run_umap_layout(args):
                       "layout_ms": round(e0.elapsed_time(e1), 3), "finite": bool(torch.isfinite(y).all().item())}))
 
 
+def run_knn_scores(args):
+    """The precision self-kNN on a config's PCA scores (--knn-source c1/c2/c3):
+    make_graph's own scores, once with the queries being the references (the
+    locality order applies) and once with a copy of them as the queries (it
+    does not); W warm-up calls and one more of each, CUDA-event timed."""
+    import torch
+    from scarf_gb300 import kernels as K
+    from scarf_gb300 import pipeline
+    cfg = CONFIGS[args.knn_source]
+    dev = torch.device("cuda", 0)
+    csr, feat = make_input(cfg, dev)
+    ip, ind, dat = (torch.from_numpy(a).to(dev) for a in (csr.indptr, csr.indices, csr.data))
+    g = pipeline.make_graph(ip, ind, dat, csr.n_genes, feat, cfg["dims"], cfg["k"], batch_size=BATCH,
+                            precision="precision", smooth=False, keep_x=False, autotune=False)
+    del ip, ind, dat
+    s = g.scores
+    out = {"mode": "knn", "source": args.knn_source, "rows": int(s.shape[0])}
+    for name, q in (("self_locality", s), ("copy_no_locality", s.clone())):
+        for _ in range(args.warmup):
+            K.knn(q, s, g.dims, g.k, self_offset=0, margin=16, precision="precision")
+        K.profile(True)
+        K.profile_reset()
+        idx, _, nm = K.knn(q, s, g.dims, g.k, self_offset=0, margin=16, precision="precision")
+        torch.cuda.synchronize()
+        t, _ = K.profile_query("knn_tc")
+        K.profile(False)
+        out[name] = {"knn_tc_ms": round(t, 3), "splits": K.knn_last_splits(),
+                     "locality_order": bool(K.knn_last_locality()), "missed": int(nm.item())}
+        out.setdefault("_idx", []).append(idx)
+    out["same_neighbours"] = bool(torch.equal(out["_idx"][0], out["_idx"][1]))
+    del out["_idx"]
+    print(json.dumps(out), flush=True)
+
+
 def run_knn(args):
     """The kNN kernel alone (profiling case): seeded clustered points (40
     centres, N(0, 1) offsets, d = 50), the first --knn-queries rows against
     all --knn-refs rows, k = 21, margin 16, the precision form; W warm-up
-    calls and one more."""
+    calls and one more. With --knn-source, a config's PCA scores instead
+    (run_knn_scores)."""
     import torch
     import __graft_entry__
     __graft_entry__.build()
+    if args.knn_source:
+        return run_knn_scores(args)
     from scarf_gb300 import kernels as K
     dev = torch.device("cuda", 0)
     g = torch.Generator(device="cuda").manual_seed(3)
