@@ -12,8 +12,6 @@
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
-#include "la.cuh"
-
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -506,19 +504,21 @@ namespace {
 // values, both in ascending order. When `resid` is given, it receives
 // max_c ||A v_c - w_c v_c|| / max|w| over the top n_top Ritz pairs (host value;
 // this synchronises the stream).
-int rayleigh_ritz_fp64(sg_handle* h, const double* A, int n, int m, double* Q, double* Y, double* V, double* G,
-                       double* B, double* W, int* info, int n_top, double* resid, double* rcol, double* gsc,
-                       cudaStream_t st) {
+int rayleigh_ritz_fp64(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, const double* A, int n, int m,
+                       double* Q, double* Y, double* V, double* G, double* B, double* W, int* info, int lwork_d,
+                       int n_top, double* resid, double* rcol, cudaStream_t st) {
+  const double one = 1.0, zero = 0.0;
   sg::ProfScope prof(h, "eig_rr64", st);
   // Q <- Q R^-1 with Q^T Q = L L^T (R = L^T): FP64 Cholesky-QR
-  int rc = sg::la::gemm<double>(true, m, m, n, 1.0, Q, n, Q, n, 0.0, G, m, gsc, st);
-  if (!rc) rc = sg::la::potrf<double>(m, G, m, info, st);
-  if (!rc) rc = sg::la::trsm_rlt<double>(n, m, G, m, Q, st);
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Q, n, Q, n, &zero, G, m));
+  SG_SOLVER(cusolverDnDpotrf(sol, CUBLAS_FILL_MODE_LOWER, m, G, m, static_cast<double*>(h->solver_work),
+                             int(h->solver_work_bytes / sizeof(double)), info));
+  SG_BLAS(cublasDtrsm(blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, m, &one, G,
+                      m, Q, n));
   // Rayleigh quotient B = Q^T A Q and its FP64 eigendecomposition, on the
   // host: at these sizes a device solver is bound by launch latency
-  if (!rc) rc = sg::la::gemm<double>(false, n, m, n, 1.0, A, n, Q, n, 0.0, Y, n, gsc, st);
-  if (!rc) rc = sg::la::gemm<double>(true, m, m, n, 1.0, Q, n, Y, n, 0.0, B, m, gsc, st);
-  if (rc) return rc;
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, &one, A, n, Q, n, &zero, Y, n));
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Q, n, Y, n, &zero, B, m));
   {
     const size_t mm = static_cast<size_t>(m) * static_cast<size_t>(m);
     std::vector<double> hb(mm), hu(mm), hw(static_cast<size_t>(m));
@@ -530,12 +530,11 @@ int rayleigh_ritz_fp64(sg_handle* h, const double* A, int n, int m, double* Q, d
     SG_CUDA(cudaMemcpyAsync(W, hw.data(), sizeof(double) * size_t(m), cudaMemcpyHostToDevice, st));
     SG_CUDA(cudaStreamSynchronize(st));  // the host buffers go out of scope
   }
-  rc = sg::la::gemm<double>(false, n, m, m, 1.0, Q, n, B, m, 0.0, V, n, gsc, st);
-  if (rc) return rc;
+  (void)lwork_d;
+  SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, Q, n, B, m, &zero, V, n));
   if (resid) {
     // A V = (A Q) U; the residual of Ritz pair c is (A Q) u_c - w_c v_c
-    rc = sg::la::gemm<double>(false, n, m, m, 1.0, Y, n, B, m, 0.0, Q, n, gsc, st);
-    if (rc) return rc;
+    SG_BLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, Y, n, B, m, &zero, Q, n));
     ritz_residual_kernel<<<n_top, 256, 0, st>>>(Q + size_t(m - n_top) * n, V + size_t(m - n_top) * n, W + (m - n_top),
                                                 W + (m - 1), n, rcol);
     SG_LAUNCH_CHECK();
@@ -547,11 +546,6 @@ int rayleigh_ritz_fp64(sg_handle* h, const double* A, int n, int m, double* Q, d
     *resid = mx;
   }
   return SG_OK;
-}
-
-// scratch (elements) of the FP64 Rayleigh-Ritz GEMMs on an n x m block
-size_t rr64_scratch(int n, int m) {
-  return std::max({sg::la::gemm_scratch(m, m, n), sg::la::gemm_scratch(n, m, n), sg::la::gemm_scratch(n, m, m)});
 }
 
 int check_info(const int* info, int count, cudaStream_t st, const char* what) {
@@ -607,17 +601,14 @@ extern "C" int sg_pca_basis_mixed(sg_handle* h, const double* cov, const double*
   int rc = solver_handles(h, st, &sol, &blas);
   if (rc) return rc;
   const size_t nn = size_t(n) * n, nm = size_t(n) * m, mm = size_t(m) * m;
-  const size_t gs = rr64_scratch(n, m);
   const size_t need = sg::Carver::need(nn * 8) + sg::Carver::need(nn * 4) + 3 * sg::Carver::need(nm * 8) +
-                      2 * sg::Carver::need(mm * 8) + 2 * sg::Carver::need(size_t(n) * 8) + sg::Carver::need(gs * 8) +
-                      1024;
+                      2 * sg::Carver::need(mm * 8) + 2 * sg::Carver::need(size_t(n) * 8) + 1024;
   int status;
   void* w = sg::ws_get(h, need, &status);
   if (!w) return status;
   sg::Carver cv(w);
   double* A = cv.take<double>(nn);
   float* A32 = cv.take<float>(nn);
-  double* gsc = cv.take<double>(std::max<size_t>(gs, 1));
   double* Q = cv.take<double>(nm);
   double* Y = cv.take<double>(nm);
   double* V = cv.take<double>(nm);
@@ -640,7 +631,9 @@ extern "C" int sg_pca_basis_mixed(sg_handle* h, const double* cov, const double*
   int meig = 0, lwork = 0;
   SG_SOLVER(cusolverDnSsyevdx_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER,
                                          n, A32, n, 0.f, 0.f, il, iu, &meig, W32, &lwork));
-  const size_t wb = sizeof(float) * size_t(lwork);
+  int lwork_d = 0;
+  SG_SOLVER(cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, B, m, W, &lwork_d));
+  const size_t wb = std::max(sizeof(float) * size_t(lwork), sizeof(double) * size_t(lwork_d));
   rc = solver_work(h, wb);
   if (rc) return rc;
   SG_SOLVER(cusolverDnSsyevdx(sol, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_I, CUBLAS_FILL_MODE_LOWER, n, A32, n,
@@ -648,7 +641,7 @@ extern "C" int sg_pca_basis_mixed(sg_handle* h, const double* cov, const double*
   if (meig != m) return sg::fail(SG_ERR_CUDA, "cusolverDnSsyevdx returned %d of %d eigenpairs", meig, m);
   f32_to_f64_kernel<<<sg::ceil_div_i(int64_t(nm), 256), 256, 0, st>>>(A32, Q, int64_t(nm));
   SG_LAUNCH_CHECK();
-  rc = rayleigh_ritz_fp64(h, A, n, m, Q, Y, V, G, B, W, info, n_comp, nullptr, nullptr, gsc, st);
+  rc = rayleigh_ritz_fp64(h, sol, blas, A, n, m, Q, Y, V, G, B, W, info, lwork_d, n_comp, nullptr, nullptr, st);
   if (rc) return rc;
   rc = check_info(info, 3, st, "sg_pca_basis_mixed");
   if (rc) return rc;
@@ -781,35 +774,25 @@ struct FilterBufs {
   float* P;   // n x m scratch
   float* Q;   // n x m scratch
   float* G;   // m x m
-  float* V;   // m x m eigenvectors of the Rayleigh quotient
-  float* Vj;  // m x m Jacobi scratch (blocks wider than 192)
   float* W;   // m Ritz values
   float* D;   // m diagonal of the Gram matrix
   float* R;   // Rayleigh quotients of the last columns
-  float* gs;  // split-K scratch of the FP32 GEMMs
   int* info;  // one slot per factorisation
   int n_info;
   int cap_info;
 };
-
-// split-K scratch (floats) of the filter's FP32 GEMMs on an n x m block
-size_t filter_gemm_scratch(int n, int m) {
-  size_t s = 0;
-  for (int w : {m, m - 1})  // the full block and the block beside a locked vector
-    s = std::max({s, sg::la::gemm_scratch(n, w, n), sg::la::gemm_scratch(w, w, n), sg::la::gemm_scratch(n, w, w)});
-  return s;
-}
 
 // Y <- Y D L^-T with (Y D)^T (Y D) = L L^T and D the column scaling, in place
 // (FP32 Cholesky-QR on unit-norm columns), `passes` times. The first columns
 // keep their span: the block stays ordered with its dominant directions
 // first. One pass leaves the columns orthogonal to ~u cond(Y)^2, enough
 // between filter segments; two passes make them orthonormal to FP32.
-int cholqr_f32(sg_handle* h, float* Y, int n, int m, FilterBufs& b, int passes, cudaStream_t st) {
+int cholqr_f32(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, float* Y, int n, int m, FilterBufs& b,
+               int passes, cudaStream_t st) {
+  const float one = 1.f, zero = 0.f;
   sg::ProfScope prof(h, "eig_qr", st);
   for (int pass = 0; pass < passes; ++pass) {
-    int rc = sg::la::gemm<float>(true, m, m, n, 1.f, Y, n, Y, n, 0.f, b.G, m, b.gs, st);
-    if (rc) return rc;
+    SG_BLAS(cublasSgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, Y, n, Y, n, &zero, b.G, m));
     int* inf = b.info + std::min(b.n_info, b.cap_info - 3);
     ++b.n_info;
     diag_copy_kernel<<<sg::ceil_div_i(m, 256), 256, 0, st>>>(b.G, b.D, m);
@@ -818,20 +801,23 @@ int cholqr_f32(sg_handle* h, float* Y, int n, int m, FilterBufs& b, int passes, 
     SG_LAUNCH_CHECK();
     col_rscale_kernel<<<sg::ceil_div_i(int64_t(n) * m, 256), 256, 0, st>>>(Y, b.D, n, m);
     SG_LAUNCH_CHECK();
-    rc = sg::la::potrf<float>(m, b.G, m, inf, st);
-    if (!rc) rc = sg::la::trsm_rlt<float>(n, m, b.G, m, Y, st);
-    if (rc) return rc;
+    SG_SOLVER(cusolverDnSpotrf(sol, CUBLAS_FILL_MODE_LOWER, m, b.G, m, static_cast<float*>(h->solver_work),
+                               int(h->solver_work_bytes / sizeof(float)), inf));
+    SG_BLAS(cublasStrsm(blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, m, &one,
+                        b.G, m, Y, n));
   }
   return SG_OK;
 }
 
 constexpr int kTailCols = 8;
 
-// C = alpha A B + beta C for the filter's n x n by n x m products (FP32 SIMT
-// tiles, the split of K reduced in a fixed order)
-int filter_gemm(int n, int m, float alpha, const float* A, const float* B, float beta, float* C, float* gs,
-                cudaStream_t st) {
-  return sg::la::gemm<float>(false, n, m, n, alpha, A, n, B, n, beta, C, n, gs, st);
+// C = alpha A B + beta C for the filter's n x n by n x m products: FP32 inputs
+// and outputs, computed by cuBLAS as FP32 emulated with BF16 splits on the
+// tensor cores (the accuracy of an FP32 GEMM, about 20% faster here)
+cublasStatus_t filter_gemm(cublasHandle_t blas, int n, int m, const float* alpha, const float* A, const float* B,
+                           const float* beta, float* C) {
+  return cublasGemmEx(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, n, alpha, A, CUDA_R_32F, n, B, CUDA_R_32F, n, beta, C,
+                      CUDA_R_32F, n, CUBLAS_COMPUTE_32F_EMULATED_16BFX9, CUBLAS_GEMM_DEFAULT);
 }
 
 // One filter segment on the block X: X <- orth(T_deg((2A - cut I)/cut) X),
@@ -839,28 +825,26 @@ int filter_gemm(int n, int m, float alpha, const float* A, const float* B, float
 // above it. Recurrence: Y1 = (2/cut) A X - X, Y_{k+1} = (4/cut) A Y_k - 2 Y_k - Y_{k-1}.
 // *tail_rq receives the smallest Rayleigh quotient of the input block's last
 // kTailCols columns (host value; synchronises).
-int filter_segment(sg_handle* h, const float* A32, int n, int m, int deg, double cut, FilterBufs& b, cudaStream_t st,
-                   float* tail_rq, int qr_passes) {
-  const float a1 = float(2.0 / cut), a2 = float(4.0 / cut);
+int filter_segment(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, const float* A32, int n, int m, int deg,
+                   double cut, FilterBufs& b, cudaStream_t st, float* tail_rq, int qr_passes) {
+  const float a1 = float(2.0 / cut), a2 = float(4.0 / cut), m1 = -1.f, m2 = -2.f, one = 1.f;
   float* prev = b.X;
   float* cur = b.P;
   const int K = std::min(kTailCols, m);
   {
     sg::ProfScope prof_f(h, "eig_filter", st);
     SG_CUDA(cudaMemcpyAsync(cur, prev, sizeof(float) * size_t(n) * m, cudaMemcpyDeviceToDevice, st));
-    int rc = filter_gemm(n, m, a1, A32, prev, -1.f, cur, b.gs, st);
-    if (rc) return rc;
+    SG_BLAS(filter_gemm(blas, n, m, &a1, A32, prev, &m1, cur));
     tail_rq_kernel<<<K, 256, 0, st>>>(prev, cur, n, m, K, a1, b.R);
     SG_LAUNCH_CHECK();
     for (int k = 2; k <= deg; ++k) {
       // prev <- -prev - 2 cur, then prev <- (4/cut) A cur + prev
-      rc = sg::la::cheb_combine_f32(int64_t(n) * m, prev, cur, st);
-      if (!rc) rc = filter_gemm(n, m, a2, A32, cur, 1.f, prev, b.gs, st);
-      if (rc) return rc;
+      SG_BLAS(cublasSgeam(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, &m1, prev, n, &m2, cur, n, prev, n));
+      SG_BLAS(filter_gemm(blas, n, m, &a2, A32, cur, &one, prev));
       std::swap(prev, cur);
     }
   }
-  int rc = cholqr_f32(h, cur, n, m, b, qr_passes, st);
+  int rc = cholqr_f32(h, sol, blas, cur, n, m, b, qr_passes, st);
   if (rc) return rc;
   // the tail quotients are read once the segment's work is queued
   float hr[kTailCols];
@@ -879,22 +863,21 @@ int filter_segment(sg_handle* h, const float* A32, int n, int m, int deg, double
 
 // FP32 Rayleigh-Ritz of the block: X <- X U (Ritz vectors, descending: the
 // dominant directions first); the Ritz values, ascending, are copied to `wh`
-// (host, synchronising). The m x m eigenproblem is the one-CTA Jacobi solver.
-int ritz_f32(sg_handle* h, const float* A32, int n, int m, FilterBufs& b, std::vector<float>& wh, bool vectors,
-             cudaStream_t st) {
+// (host, synchronising).
+int ritz_f32(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, const float* A32, int n, int m, FilterBufs& b,
+             int lwork_s, std::vector<float>& wh, bool vectors, cudaStream_t st) {
+  const float one = 1.f, zero = 0.f;
   sg::ProfScope prof(h, "eig_rr32", st);
-  int rc = filter_gemm(n, m, 1.f, A32, b.X, 0.f, b.P, b.gs, st);
-  if (!rc) rc = sg::la::gemm<float>(true, m, m, n, 1.f, b.X, n, b.P, n, 0.f, b.G, m, b.gs, st);
-  if (rc) return rc;
+  SG_BLAS(filter_gemm(blas, n, m, &one, A32, b.X, &zero, b.P));
+  SG_BLAS(cublasSgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, b.X, n, b.P, n, &zero, b.G, m));
   int* inf = b.info + std::min(b.n_info, b.cap_info - 1);
   ++b.n_info;
-  rc = sg::la::syev_f32(m, b.G, m, b.W, b.V, b.Vj, inf, st);
-  if (rc) return rc;
+  SG_SOLVER(cusolverDnSsyevd(sol, vectors ? CUSOLVER_EIG_MODE_VECTOR : CUSOLVER_EIG_MODE_NOVECTOR,
+                             CUBLAS_FILL_MODE_LOWER, m, b.G, m, b.W, static_cast<float*>(h->solver_work), lwork_s, inf));
   if (vectors) {
-    reverse_cols_kernel<<<sg::ceil_div_i(int64_t(m / 2) * m, 256), 256, 0, st>>>(b.V, m);
+    reverse_cols_kernel<<<sg::ceil_div_i(int64_t(m / 2) * m, 256), 256, 0, st>>>(b.G, m);
     SG_LAUNCH_CHECK();
-    rc = sg::la::gemm<float>(false, n, m, m, 1.f, b.X, n, b.V, m, 0.f, b.P, n, b.gs, st);
-    if (rc) return rc;
+    SG_BLAS(cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, n, m, m, &one, b.X, n, b.G, m, &zero, b.P, n));
     std::swap(b.X, b.P);
   }
   wh.resize(size_t(m));
@@ -942,14 +925,16 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
   if (m > 256 || 2 * m > n || n_used < 4 * int64_t(m))
     return sg_pca_basis_mixed(h, cov, zsum, n_used, n_cols, n_comp, comps, evals, evr, n_load, loadings32, ld_l,
                               stream);
-  int rc = SG_OK;
+  cusolverDnHandle_t sol;
+  cublasHandle_t blas;
+  int rc = solver_handles(h, st, &sol, &blas);
+  if (rc) return rc;
   const size_t nn = size_t(n) * n, nm = size_t(n) * m, np = size_t(n) * p, pp = size_t(p) * p;
   const int cap_info = 128;
-  const size_t gs = filter_gemm_scratch(n, m), gsd = rr64_scratch(n, p);
   const size_t need = sg::Carver::need(nn * 8) + sg::Carver::need(nn * 4) + 3 * sg::Carver::need(nm * 4) +
-                      3 * sg::Carver::need(size_t(m) * m * 4) + 2 * sg::Carver::need(size_t(m) * 4) +
+                      sg::Carver::need(size_t(m) * m * 4) + 2 * sg::Carver::need(size_t(m) * 4) +
                       sg::Carver::need(kTailCols * 4) + sg::Carver::need(nn * 4) + sg::Carver::need(size_t(n) * 12) +
-                      sg::Carver::need(8) + sg::Carver::need(gs * 4 + 4) + sg::Carver::need(gsd * 8 + 8) +
+                      sg::Carver::need(8) +
                       3 * sg::Carver::need(np * 8) + 2 * sg::Carver::need(pp * 8) + sg::Carver::need(size_t(p) * 8) +
                       sg::Carver::need(size_t(p) * 8) + sg::Carver::need(16) + sg::Carver::need(cap_info * 4);
   int status;
@@ -963,10 +948,6 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
   b.P = cv.take<float>(nm);
   b.Q = cv.take<float>(nm);
   b.G = cv.take<float>(size_t(m) * m);
-  b.V = cv.take<float>(size_t(m) * m);
-  b.Vj = cv.take<float>(size_t(m) * m);
-  b.gs = cv.take<float>(gs + 1);
-  double* gsc = cv.take<double>(gsd + 1);
   b.W = cv.take<float>(size_t(m));
   b.D = cv.take<float>(size_t(m));
   b.R = cv.take<float>(size_t(kTailCols));
@@ -999,7 +980,17 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
   SG_LAUNCH_CHECK();
   random_block_kernel<<<sg::ceil_div_i(int64_t(nm), 256), 256, 0, st>>>(b.X, int64_t(nm), 0x5CA2F00Dull);
   SG_LAUNCH_CHECK();
-  rc = cholqr_f32(h, b.X, n, m, b, 2, st);
+  // workspace: FP32 potrf / syevd of m, FP64 potrf / syevd of p
+  int lw_potrf = 0, lw_s = 0, lw_d = 0, lw_dp = 0;
+  SG_SOLVER(cusolverDnSpotrf_bufferSize(sol, CUBLAS_FILL_MODE_LOWER, m, b.G, m, &lw_potrf));
+  SG_SOLVER(cusolverDnSsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, b.G, m, b.W, &lw_s));
+  SG_SOLVER(cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, p, Bd, p, Wd, &lw_d));
+  SG_SOLVER(cusolverDnDpotrf_bufferSize(sol, CUBLAS_FILL_MODE_LOWER, p, Gd, p, &lw_dp));
+  const size_t wb = std::max(std::max(sizeof(float) * size_t(lw_potrf), sizeof(float) * size_t(lw_s)),
+                             std::max(sizeof(double) * size_t(lw_d), sizeof(double) * size_t(lw_dp)));
+  rc = solver_work(h, wb);
+  if (rc) return rc;
+  rc = cholqr_f32(h, sol, blas, b.X, n, m, b, 2, st);
   if (rc) return rc;
   double hd[2];
   SG_CUDA(cudaMemcpyAsync(hd, tr, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1013,12 +1004,12 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
   EIG_DBG("filter: n=%d m=%d p=%d trace/n=%g rowmax=%g degA=%d\n", n, m, p, cut, double(hrow), deg);
   float rq = 0.f;
   for (int s = 0; s < 2; ++s) {  // the second leaves X orthonormal for the Rayleigh-Ritz step
-    rc = filter_segment(h, A32, n, m, deg, cut, b, st, &rq, s == 1 ? 2 : 1);
+    rc = filter_segment(h, sol, blas, A32, n, m, deg, cut, b, st, &rq, s == 1 ? 2 : 1);
     if (rc) return rc;
   }
   // phase B: cut from the block's smallest Ritz value, degree from its largest
   std::vector<float> th;
-  rc = ritz_f32(h, A32, n, m, b, th, true, st);
+  rc = ritz_f32(h, sol, blas, A32, n, m, b, lw_s, th, true, st);
   if (rc) return rc;
   bool ok = th[0] > 0.f && std::isfinite(th[size_t(m - 1)]);
   EIG_DBG("filter: RR1 ok=%d theta_min=%g theta_max=%g\n", int(ok), double(th[0]), double(th[size_t(m - 1)]));
@@ -1051,6 +1042,7 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
       const double t1 = double(th[size_t(m - 1)]), t2 = double(th[size_t(m - 2)]);
       if (2.0 * t1 / cut - 1.0 > 3.0 && t1 >= 1.5 * t2 && n_comp >= 2) L = 1;
       if (L) {
+        const float one = 1.f, zero = 0.f, mtwo = -2.f, mone = -1.f;
         float* v = lv;
         float* y0 = lv + n;
         float* y1 = lv + 2 * n;
@@ -1061,21 +1053,19 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
         // y0 = v, y1 = (2/c) A v - v, y_{k+1} = (4/c) A y_k - 2 y_k - y_{k-1}
         SG_CUDA(cudaMemcpyAsync(y0, v, sizeof(float) * size_t(n), cudaMemcpyDeviceToDevice, st));
         SG_CUDA(cudaMemcpyAsync(y1, v, sizeof(float) * size_t(n), cudaMemcpyDeviceToDevice, st));
-        rc = sg::la::symv_f32(n, a1, A32, v, -1.f, y1, st);
-        if (rc) return rc;
+        SG_BLAS(cublasSgemv(blas, CUBLAS_OP_N, n, n, &a1, A32, n, v, 1, &mone, y1, 1));
         float* pr = y0;
         float* cr = y1;
         for (int k = 2; k <= dl; ++k) {
-          rc = sg::la::cheb_combine_f32(n, pr, cr, st);
-          if (!rc) rc = sg::la::symv_f32(n, a2, A32, cr, 1.f, pr, st);
-          if (rc) return rc;
+          SG_BLAS(cublasSscal(blas, n, &mone, pr, 1));
+          SG_BLAS(cublasSaxpy(blas, n, &mtwo, cr, 1, pr, 1));
+          SG_BLAS(cublasSgemv(blas, CUBLAS_OP_N, n, n, &a2, A32, n, cr, 1, &one, pr, 1));
           std::swap(pr, cr);
         }
         SG_CUDA(cudaMemcpyAsync(v, cr, sizeof(float) * size_t(n), cudaMemcpyDeviceToDevice, st));
         normalize_rq_kernel<<<1, 1024, 0, st>>>(v, v, n, lrq + 1);  // unit length
         SG_LAUNCH_CHECK();
-        rc = sg::la::symv_f32(n, 1.f, A32, v, 0.f, y0, st);
-        if (rc) return rc;
+        SG_BLAS(cublasSgemv(blas, CUBLAS_OP_N, n, n, &one, A32, n, v, 1, &zero, y0, 1));
         normalize_rq_kernel<<<1, 1024, 0, st>>>(v, y0, n, lrq);  // Rayleigh quotient of the unit vector
         SG_LAUNCH_CHECK();
         float hrq = 0.f;
@@ -1085,8 +1075,9 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
           L = 0;
         } else {
           // deflated operator A - theta v v^T, and the active block X[:, 1:m]
-          rc = sg::la::syr_f32(n, A32, -hrq, v, A32d, st);
-          if (rc) return rc;
+          SG_CUDA(cudaMemcpyAsync(A32d, A32, sizeof(float) * nn, cudaMemcpyDeviceToDevice, st));
+          const float mth = -hrq;
+          SG_BLAS(cublasSger(blas, n, n, &mth, v, 1, v, 1, A32d, n));
           SG_CUDA(cudaMemcpyAsync(b.P, b.X + n, sizeof(float) * size_t(n) * (m - 1), cudaMemcpyDeviceToDevice, st));
           std::swap(b.X, b.P);
           Aop = A32d;
@@ -1109,7 +1100,7 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
       const double t_max = 2.0 * theta_max / cut - 1.0;
       const bool last = gain >= target;
       const int d = cheb_degree(t_max, last ? 1e2 : 1e5, 8);
-      rc = filter_segment(h, Aop, n, ma, d, cut, b, st, &rq, last && polish == 1 ? 2 : 1);
+      rc = filter_segment(h, sol, blas, Aop, n, ma, d, cut, b, st, &rq, last && polish == 1 ? 2 : 1);
       if (rc) return rc;
       if (!last) {
         gain += d * std::acosh(std::max(1.0, 2.0 * theta_c / cut - 1.0));
@@ -1121,9 +1112,9 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
         // below the block's tail: fresh Ritz values (of the orthonormalised
         // block, which they also put in descending order) give a higher,
         // still valid cap and a better rate estimate.
-        rc = cholqr_f32(h, b.X, n, ma, b, 1, st);
+        rc = cholqr_f32(h, sol, blas, b.X, n, ma, b, 1, st);
         if (rc) return rc;
-        rc = ritz_f32(h, Aop, n, ma, b, th, true, st);
+        rc = ritz_f32(h, sol, blas, Aop, n, ma, b, lw_s, th, true, st);
         if (rc) return rc;
         refreshed = true;
         if (th[0] > 0.f && std::isfinite(th[size_t(ma - 1)])) {
@@ -1145,16 +1136,16 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
       SG_CUDA(cudaMemcpyAsync(b.P, lv, sizeof(float) * size_t(n), cudaMemcpyDeviceToDevice, st));
       SG_CUDA(cudaMemcpyAsync(b.P + n, b.X, sizeof(float) * size_t(n) * ma, cudaMemcpyDeviceToDevice, st));
       std::swap(b.X, b.P);
-      rc = cholqr_f32(h, b.X, n, m, b, 2, st);
+      rc = cholqr_f32(h, sol, blas, b.X, n, m, b, 2, st);
       if (rc) return rc;
     }
-    rc = ritz_f32(h, A32, n, m, b, th, true, st);
+    rc = ritz_f32(h, sol, blas, A32, n, m, b, lw_s, th, true, st);
     if (rc) return rc;
     // the top p Ritz vectors (the first p columns) -> FP64 Rayleigh-Ritz with a residual check
     f32_to_f64_kernel<<<sg::ceil_div_i(int64_t(np), 256), 256, 0, st>>>(b.X, Qd, int64_t(np));
     SG_LAUNCH_CHECK();
-    rc = rayleigh_ritz_fp64(h, A, n, p, Qd, Yd, Vd, Gd, Bd, Wd, b.info + cap_info - 2, n_comp, &resid, rcol, gsc,
-                            st);
+    rc = rayleigh_ritz_fp64(h, sol, blas, A, n, p, Qd, Yd, Vd, Gd, Bd, Wd, b.info + cap_info - 2, lw_d, n_comp,
+                            &resid, rcol, st);
     if (rc) return rc;
     std::vector<int> hi(static_cast<size_t>(cap_info));
     SG_CUDA(cudaMemcpyAsync(hi.data(), b.info, sizeof(int) * cap_info, cudaMemcpyDeviceToHost, st));

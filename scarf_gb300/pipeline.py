@@ -20,6 +20,8 @@ import torch
 from . import kernels as K
 
 PLAIN_MARGIN = 0
+# rows per FP32 slice of sg_normalize_csr's column statistics
+STAT_ROWS = 256
 PRECISION_MARGIN = 16
 # covariance forms with a kernel in this build
 COV_FORMS = ("plain", "precision")
@@ -78,7 +80,8 @@ def normalize_csr_host(indptr, indices, data, n_genes: int, feat_idx, *, size_fa
     """a1+a3 over host (ideally pinned) CSR arrays. With ``chunk_cells`` the rows
     are streamed: chunk i+1 is copied on a side stream while chunk i is
     normalised. Host inputs are streamed in about 8 chunks unless
-    ``chunk_cells`` says otherwise (0: one copy). Returns ``(x, colsum, colsumsq)``."""
+    ``chunk_cells`` says otherwise (0: one copy); chunks are whole multiples
+    of the 256-row statistics slices. Returns ``(x, colsum, colsumsq)``."""
     dev = torch.device(device)
     h = len(feat_idx)
     n = len(indptr) - 1
@@ -98,6 +101,10 @@ def normalize_csr_host(indptr, indices, data, n_genes: int, feat_idx, *, size_fa
         dat_h = dat_h.to(torch.int32)
     if chunk_cells is None and ind_h.device.type == "cpu":
         chunk_cells = max(16384, -(-n // 8))
+    if chunk_cells:
+        # whole slices of the column-statistics pass (256 rows): the streamed
+        # sums then add the same FP32 slice partials as one pass over all rows
+        chunk_cells = -(-int(chunk_cells) // STAT_ROWS) * STAT_ROWS
     if not chunk_cells or chunk_cells >= n:
         ip = ip_h.to(dev, non_blocking=True)
         ind = ind_h.to(dev, non_blocking=True)
