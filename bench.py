@@ -151,13 +151,16 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
 
 
-# DRAM bytes (read + write) per launch from one ncu capture of the full-size
-# C2 step (dram__bytes_read.sum + dram__bytes_write.sum, one pass; the command
-# and the per-kernel table are kept under profiles/). "normalize" is the row
-# pass, the column-statistics pass and the partial reductions together.
+# DRAM bytes (read + write) per launch from one-pass ncu captures of the
+# full-size C2 and C3 steps (dram__bytes_read.sum + dram__bytes_write.sum; the
+# commands and per-kernel tables are kept under profiles/). At C2 "normalize"
+# is the row pass, the column-statistics pass and the partial reductions
+# together, and "smooth" the smoothing kernel with its two chunk kernels.
 DRAM_TRAFFIC = {
-    "c2:normalize": 3_441_743_360, "c2:zsplit": 1_596_976_448, "c2:cov_tc": 1_596_401_152,
-    "c2:project": 819_532_885, "c2:knn_tc": 25_810_858, "c2:rerank": 51_168_460, "c2:smooth": 93_267_626,
+    "c2:normalize": 3_442_579_776, "c2:zsplit": 1_596_928_704, "c2:cov_tc": 1_729_305_792,
+    "c2:project": 831_836_245, "c2:knn_tc": 25_911_808, "c2:rerank": 36_871_680, "c2:smooth": 36_306_773,
+    "c3:zsplit": 18_312_334_720, "c3:cov_tc": 53_842_151_360, "c3:project": 8_341_655_616,
+    "c3:knn_tc": 17_302_698_854, "c3:rerank": 4_295_605_350, "c3:smooth": 698_150_464,
 }
 
 
