@@ -129,7 +129,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "sm_min_mhz": min(sm) if sm else None, "reasons": sorted(reasons), "samples": len(sm)}
 
 
 # ---------------------------------------------------------------------------
@@ -454,7 +454,10 @@ def run_gb300(args, cfg):
     knn_layout = {"splits": K.knn_last_splits(), "locality_order": bool(K.knn_last_locality())}
     rec, werr = graph_check(res, BATCH)
     ann_recall = res.recall()
+    sampler_e2e = ClockSampler(local)
+    sampler_e2e.start()
     e2e_ms, res_h, _, _, outs = timed("precision", args.steps, args.warmup, host=True)
+    clocks_e2e = sampler_e2e.stop()
     plain_ms, res_p, _, prof_p, _ = timed("plain", max(1, min(args.steps, 3)), 1, prof=True)
     rec_p, werr_p = graph_check(res_p, BATCH)
     truth = fp64_truth(K, pipeline, ip_d, ind_d, dat_d, G, feat, dims, k, {"precision": res, "plain": res_p})
@@ -564,7 +567,7 @@ def run_gb300(args, cfg):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "host_link": link,
                 "bound_ms": round(bound_ms, 3), "frac_of_bound": round(bound_ms / e2e_ms, 4),
                 "call": "pipeline.make_graph on pinned host CSR (chunks of %s cells), outputs read back"
-                        % (chunk or "8ths of the")},
+                        % (chunk or "8ths of the"), "clocks": clocks_e2e},
         "e2e_datastore": ds_e2e,
         "serving": serving,
         "roofline": roof,

@@ -324,6 +324,27 @@ int sg_chunks_to_csr(sg_handle* h, const uint32_t* chunks, int64_t n_rows, int32
                      int32_t* indices_out, int32_t* data_out, int64_t capacity, int64_t* nnz_out,
                      void* stream);
 
+/* f2, writing -- one Blosc1 frame per chunk of device bytes, in the format
+ * scarf's create_zarr_dataset writes through numcodecs (scarf/writers.py:
+ * 58-89): LZ4 codec, blocks not split, bit shuffle (shuffle = 2), byte
+ * shuffle (1) or none (0); a one-byte type is stored unshuffled. Chunk c is
+ * src[chunk_offsets[c] - chunk_offsets[0], chunk_offsets[c + 1] -
+ * chunk_offsets[0]) (src a device pointer, chunk_offsets a host array of
+ * n_chunks + 1 non-decreasing offsets, each chunk below 2^31 - 64 bytes).
+ * blocksize: bytes per Blosc block, a multiple of typesize, at most 32768.
+ * The frames are written back to back into the host buffer frames_out
+ * (frames_capacity bytes, at least sg_blosc_encode_bound(...)), frame c at
+ * frame_offsets_out[c] (host, n_chunks + 1 entries). A block whose LZ4 stream
+ * would not be shorter than the block is stored as it is. Synchronises the
+ * stream. */
+int sg_blosc_encode(sg_handle* h, const void* src, const int64_t* chunk_offsets, int32_t n_chunks, int32_t typesize,
+                    int32_t shuffle, int32_t blocksize, void* frames_out, int64_t frames_capacity,
+                    int64_t* frame_offsets_out, void* stream);
+
+/* Host only: a frames_capacity that sg_blosc_encode always fits in (-1 for a
+ * bad argument). */
+int64_t sg_blosc_encode_bound(const int64_t* chunk_offsets, int32_t n_chunks, int32_t blocksize);
+
 /* f1 -- the MiniBatchKMeans step of make_graph (scarf/ann.py:328-346):
  * MiniBatchKMeans(n_clusters=k, random_state=seed, batch_size=block_rows)
  * partial_fit over the row blocks of x[n x d] (row stride ld, a multiple of 4)

@@ -75,6 +75,8 @@ SIGNATURES = {
     "sg_serve_destroy": (C.c_int, [vp]),
     "sg_blosc_decode": (C.c_int, [vp, vp, vp, i32, vp, i64, vp, vp]),
     "sg_chunks_to_csr": (C.c_int, [vp, vp, i64, i32, i32, i64, i64, vp, vp, vp, i64, C.POINTER(i64), vp]),
+    "sg_blosc_encode": (C.c_int, [vp, vp, vp, i32, i32, i32, i32, vp, i64, vp, vp]),
+    "sg_blosc_encode_bound": (C.c_int64, [vp, i32, i32]),
     "sg_kmeans_minibatch": (C.c_int, [vp, vp, i64, i32, i32, i32, i32, u64, vp, vp, vp]),
     "sg_calc_snn": (C.c_int, [vp, vp, i64, i32, vp, vp]),
     "sg_merge_graphs": (C.c_int, [vp, i32, vp, vp, vp, i64, i32, vp, vp, vp]),

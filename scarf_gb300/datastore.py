@@ -202,6 +202,20 @@ class DataStore:
         return cls(ip.cpu().numpy(), ind.cpu().numpy(), dat.cpu().numpy(), n_genes, gene_ids=genes, cell_ids=cells,
                    assay_name=assay_name, precision=precision, device=device, **kw)
 
+    def to_zarr(self, store: str, chunk_size=(1000, 1000)) -> None:
+        """The DataStore as a scarf zarr directory store, every chunk encoded
+        on the device (Blosc-LZ4, bit shuffle): each assay's counts as a dense
+        ``<u4`` array in chunks of ``chunk_size`` (scarf/writers.py:164-204),
+        the cell and feature tables (``cellData/{column}``,
+        ``{assay}/featureData/{column}``) and every group and dataset the graph
+        path wrote. ``DataStore.from_zarr`` reads it back."""
+        from .zarr_io import write_counts, write_group, write_table
+        write_group(store, self.z, device=self.RNA.device if hasattr(self, "RNA") else "cuda")
+        write_table(store, "cellData", self.cells)
+        for name, a in self._assays.items():
+            write_counts(store, f"{name}/counts", a.indptr, a.indices, a.data, a.n_genes, chunk_size, device=a.device)
+            write_table(store, f"{name}/featureData", a.feats, device=a.device)
+
     def _get_assay(self, name: Optional[str]):
         return self._assays[name or self._defaultAssay]
 

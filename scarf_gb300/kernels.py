@@ -391,6 +391,30 @@ def blosc_decode(frames, out: torch.Tensor, out_starts) -> torch.Tensor:
     return out
 
 
+def blosc_encode(src: torch.Tensor, chunk_offsets, typesize: int, shuffle: int = 2,
+                 blocksize: int = 32768) -> list:
+    """f2: one Blosc1/LZ4 frame (``bytes``) per chunk of the device uint8
+    buffer ``src``; chunk c is src[chunk_offsets[c]:chunk_offsets[c + 1]]
+    (see sg_blosc_encode). ``shuffle``: 2 bit, 1 byte, 0 none."""
+    _need(src, "src", torch.uint8, 1)
+    offs = np.ascontiguousarray(chunk_offsets, dtype=np.int64)
+    n = len(offs) - 1
+    if n < 0 or offs[0] < 0 or offs[-1] > src.numel() or np.any(np.diff(offs) < 0):
+        raise ValueError("chunk offsets must be non-decreasing and inside the buffer")
+    bs = max(typesize, min(32768, blocksize) // typesize * typesize)
+    lib = L.load()
+    cap = lib.sg_blosc_encode_bound(offs.ctypes.data_as(C.c_void_p), n, bs)
+    if cap < 0:
+        raise ValueError("bad chunk offsets or block size")
+    out = np.empty(max(1, cap), dtype=np.uint8)
+    fo = np.zeros(n + 1, dtype=np.int64)
+    dev = src.device
+    L.check(lib.sg_blosc_encode(handle(dev.index).ptr, _p(src), offs.ctypes.data_as(C.c_void_p), n, int(typesize),
+                                int(shuffle), bs, out.ctypes.data_as(C.c_void_p), cap,
+                                fo.ctypes.data_as(C.c_void_p), _stream(dev)))
+    return [out[fo[c]:fo[c + 1]].tobytes() for c in range(n)]
+
+
 def chunks_to_csr(chunks: torch.Tensor, n_rows: int, chunk_rows: int, chunk_cols: int, n_cols: int,
                   indptr_base: int = 0):
     """f2: CSR (indptr int64, indices int32, data int32) of one band of decoded

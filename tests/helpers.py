@@ -183,3 +183,77 @@ def blosc_frame(data: bytes, typesize: int, blocksize: int, shuffle: str = "bit"
             body += struct.pack("<i", len(c)) + c
     hdr = struct.pack("<BBBBIII", 2, 1, flags, typesize, nbytes, blocksize, base + len(body))
     return hdr + struct.pack(f"<{nblocks}i", *starts) + bytes(body)
+
+
+def lz4_check_block(src: bytes, out_len: int) -> None:
+    """Raise unless ``src`` is an LZ4 block that follows the format's
+    end-of-block rules: the last sequence is literals only, the last 5 bytes
+    of the output are literals, no match starts within the last 12 bytes,
+    offsets point inside the output and the sequences decode to ``out_len``
+    bytes."""
+    ip = op = 0
+    n = len(src)
+    while True:
+        if ip >= n:
+            raise ValueError("lz4: missing last sequence")
+        token = src[ip]
+        ip += 1
+        lit = token >> 4
+        if lit == 15:
+            while True:
+                b = src[ip]
+                ip += 1
+                lit += b
+                if b != 255:
+                    break
+        ip += lit
+        op += lit
+        if ip > n:
+            raise ValueError("lz4: literals past the end")
+        if ip == n:
+            if token & 15:
+                raise ValueError("lz4: last token announces a match")
+            break
+        off = src[ip] | (src[ip + 1] << 8)
+        ip += 2
+        mlen = (token & 15) + 4
+        if (token & 15) == 15:
+            while True:
+                b = src[ip]
+                ip += 1
+                mlen += b
+                if b != 255:
+                    break
+        if off == 0 or off > op:
+            raise ValueError("lz4: offset outside the output")
+        if op + 12 > out_len:
+            raise ValueError("lz4: a match starts within the last 12 bytes")
+        op += mlen
+        if op > out_len - 5:
+            raise ValueError("lz4: a match reaches into the last 5 bytes")
+    if op != out_len:
+        raise ValueError(f"lz4: {op} bytes, expected {out_len}")
+
+
+def check_frame(frame: bytes) -> dict:
+    """Check a Blosc1 frame's header and every LZ4 stream of its blocks
+    against the format rules; return the parsed header."""
+    import struct
+    version, vlz, flags, ts, nbytes, bsize, cbytes = struct.unpack_from("<BBBBIII", frame, 0)
+    assert cbytes == len(frame), (cbytes, len(frame))
+    assert version == 2 and vlz == 1 and (flags >> 5) == 1
+    if nbytes:
+        nb = -(-nbytes // bsize)
+        starts = struct.unpack_from(f"<{nb}i", frame, 16)
+        for b, st in enumerate(starts):
+            blen = min(bsize, nbytes - b * bsize)
+            nsplit = ts if (not (flags & 0x10) and blen == bsize) else 1
+            pos = st
+            for _ in range(nsplit):
+                cs = struct.unpack_from("<i", frame, pos)[0]
+                pos += 4
+                slen = blen // nsplit
+                if cs != slen:
+                    lz4_check_block(frame[pos:pos + cs], slen)
+                pos += cs
+    return {"flags": flags, "typesize": ts, "nbytes": nbytes, "blocksize": bsize}

@@ -13,7 +13,7 @@ HEADER = os.path.join(ROOT, "include", "scarf_gb300.h")
 
 def declared():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*|size_t|unsigned long long|double)\s+(sg_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char\*|size_t|unsigned long long|double)\s+(sg_\w+)\s*\(", text, re.M)))
 
 
 @pytest.fixture(scope="module")
@@ -28,7 +28,7 @@ def lib_path():
 def test_header_declares_entry_points():
     names = declared()
     for n in ("sg_normalize_csr", "sg_zstats", "sg_covariance", "sg_pca_basis", "sg_project", "sg_knn",
-              "sg_smooth", "sg_fuzzy_union", "sg_kmeans_minibatch", "sg_calc_snn", "sg_merge_graphs", "sg_umap_layout", "sg_create", "sg_destroy", "sg_last_error"):
+              "sg_smooth", "sg_fuzzy_union", "sg_kmeans_minibatch", "sg_blosc_decode", "sg_blosc_encode", "sg_calc_snn", "sg_merge_graphs", "sg_umap_layout", "sg_create", "sg_destroy", "sg_last_error"):
         assert n in names
 
 
