@@ -352,10 +352,13 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
     const int64_t qpos = q0 + row;
     const int64_t qout = (perm != nullptr && qpos < nq) ? int64_t(perm[qpos]) : qpos;
     int* out = cand + (int64_t(blockIdx.y) * nq_pad + qout) * KC;
+    // padding rows (index nr and up) carry enormous keys but still fill the
+    // slots of a list whose split has fewer than KC references: they are
+    // not candidates (-1, which the re-rank skips)
 #pragma unroll
     for (int j = 0; j < KC; ++j) {
       const int ix = top.i[j];
-      out[j] = (perm != nullptr && ix >= 0 && ix < nr) ? perm[ix] : ix;
+      out[j] = (ix >= 0 && ix < nr) ? (perm != nullptr ? perm[ix] : ix) : -1;
     }
   }
   __syncthreads();

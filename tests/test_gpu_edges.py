@@ -1,0 +1,108 @@
+"""Edge cases of the graph path through DataStore.make_graph, both forms,
+against the oracle: the smallest graph AnnStream allows (k = n - 1 after the
+caps of scarf/ann.py:91-92, :173-185), duplicate cells (zero distances and
+ties, where the self rule of fix_knn_query, scarf/ann.py:31-52, and rho of
+smooth_knn_dist matter), cells without any count in the selected features
+(library size 0 -> 1, scarf/assay.py:54-64) and a feature that is constant
+over the cells (sigma 0 -> 1, clean_array, scarf/utils.py:143-153)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import oracle
+from helpers import small_counts, top_var_genes
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _graph(indptr, indices, data, G, feat, form, dims, k, batch):
+    from scarf_gb300.datastore import DataStore
+    ds = DataStore(indptr, indices, data, G, precision=form)
+    mask = np.zeros(G, dtype=bool)
+    mask[feat] = True
+    ds.RNA.feats.insert("I__hvgs", mask)
+    ds.make_graph(feat_key="hvgs", dims=dims, k=k, batch_size=batch)
+    loc = ds._get_latest_graph_loc("RNA", "I", "hvgs")
+    knn = ds.zw[loc.rsplit("/", 1)[0]]
+    g = ds.zw[loc]
+    red = ds.zw["RNA/normed__I__hvgs"].attrs["latest_reduction"]
+    ann = ds._ann_cache[ds.zw[red].attrs["latest_ann"]]
+    return ds, knn, g, ann
+
+
+def _check(indptr, indices, data, G, feat, form, dims, k, batch, want_k=None):
+    ds, knn, g, ann = _graph(indptr, indices, data, G, feat, form, dims, k, batch)
+    n = len(indptr) - 1
+    gi = knn["indices"][:].astype(np.int64)
+    gd = knn["distances"][:]
+    kk = gi.shape[1]
+    if want_k is not None:
+        assert kk == want_k
+    d = ann.dims
+    s = ann.annIdx.scores[:, :d].double().cpu().numpy()
+    # the neighbours: tie-aware recall against exact FP64 kNN of the graph's own scores
+    _, ed = oracle.exact_knn(s, s, kk + 1)
+    rec = oracle.recall_at_k(s, s, gi, ed[:, -1], rel=1e-5)
+    assert rec >= 0.995, f"{form}: recall {rec}"
+    assert np.all((gi >= 0) & (gi < n))
+    # the weights: the oracle's smoothing of the same neighbours, edges bit for bit
+    e_want, w_want = oracle.smoothen_dists(gi.astype(np.uint64), gd, 1.0, 1.5, batch)
+    assert np.array_equal(g["edges"][:], e_want)
+    assert np.abs(g["weights"][:] - w_want).max() <= 1e-5
+    assert np.all(np.isfinite(g["weights"][:]))
+    # the union, bit for bit
+    gm = sp.csr_matrix((g["weights"][:], (g["edges"][:, 0].astype(np.int64), g["edges"][:, 1].astype(np.int64))),
+                       shape=(n, n))
+    u_want = oracle.symmetrize(gm)
+    u_want.sort_indices()
+    u = ds.load_graph(feat_key="hvgs", symmetric=True)
+    assert np.array_equal(u.indptr, u_want.indptr) and np.array_equal(u.indices, u_want.indices)
+    assert np.array_equal(u.data, u_want.data)
+    return ds, gi, gd
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+@pytest.mark.parametrize("form", ["plain", "precision"])
+def test_smallest_graph(gpu, form):
+    # 14 cells, k = 21 asked: AnnStream caps k at n - 1 = 13 and dims at n
+    indptr, indices, data, G, _ = small_counts(n_cells=14, n_genes=400, seed=3)
+    feat = top_var_genes(indptr, indices, data, G, 50)
+    _check(indptr, indices, data, G, feat, form, dims=10, k=21, batch=14, want_k=13)
+
+
+@pytest.mark.parametrize("form", ["plain", "precision"])
+def test_duplicate_cells_and_empty_feature_rows(gpu, form):
+    indptr, indices, data, G, _ = small_counts(n_cells=900, n_genes=1500, seed=8)
+    m = sp.csr_matrix((data, indices, indptr), shape=(len(indptr) - 1, G)).tolil()
+    feat = top_var_genes(indptr, indices, data, G, 120)
+    other = np.setdiff1d(np.arange(G), feat)
+    # cells 10..14 copy cell 5; cells 20..27 have counts only outside the features
+    for r in range(10, 15):
+        m[r] = m[5]
+    for r in range(20, 28):
+        m[r] = 0
+        m[r, other[r]] = 4
+    # a feature no cell has a count of: constant over the cells, sigma 0
+    m[:, feat[0]] = 0
+    c = m.tocsr()
+    c.sort_indices()
+    ds, gi, gd = _check(c.indptr.astype(np.int64), c.indices.astype(np.int32), c.data.astype(np.int32), G, feat,
+                        form, dims=15, k=11, batch=300)
+    # the copies of cell 5 find one another at distance 0
+    for r in (5, 10, 11, 12, 13, 14):
+        dup = {5, 10, 11, 12, 13, 14} - {r}
+        assert dup <= set(gi[r].tolist()), (r, gi[r])
+        assert np.all(gd[r][np.isin(gi[r], list(dup))] <= 1e-6)
+    # the cells without feature counts (and the empty cells 3 and 700) are identical in the reduced
+    # space: one zero-distance clique of 10, within every member's 11 neighbours
+    zero = set(range(20, 28)) | {3, 700}
+    for r in sorted(zero):
+        assert zero - {r} <= set(gi[r].tolist()), (r, gi[r])
+    sig = ds.zw["RNA/normed__I__hvgs"]["sigma"][:]
+    assert np.all(np.isfinite(sig)) and np.all(sig > 0)
