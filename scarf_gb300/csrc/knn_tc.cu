@@ -276,7 +276,7 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
 #pragma unroll
       for (int q = 0; q < 32; ++q) {
         float key = __uint_as_float(r[q]);
-        if (kRn) key = fmaf(-2.f, key, my_rn[ch * 32 + q]);
+        if (kRn) key += my_rn[ch * 32 + q];  // the accumulator is -2 q.r (the queries are scaled by -2)
         kk[q] = key;
       }
       float m8[4];
@@ -309,7 +309,10 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
         const int b = t & 1;
         const uint32_t aph = (t >> 1) & 1;
         const int64_t r0 = tile_at(t);
-        if (kRn) reinterpret_cast<float4*>(my_rn)[lane] = __ldg(reinterpret_cast<const float4*>(rn + r0) + lane);
+        if (kRn) {
+          __syncwarp();  // every lane has read the last tile's norms
+          reinterpret_cast<float4*>(my_rn)[lane] = __ldg(reinterpret_cast<const float4*>(rn + r0) + lane);
+        }
         if (SHARE) {
           shared = fminf(shared, bits_key(__ldcg(qb)));
           thr = fminf(thr, shared);

@@ -106,3 +106,27 @@ def test_duplicate_cells_and_empty_feature_rows(gpu, form):
         assert zero - {r} <= set(gi[r].tolist()), (r, gi[r])
     sig = ds.zw["RNA/normed__I__hvgs"]["sigma"][:]
     assert np.all(np.isfinite(sig)) and np.all(sig > 0)
+
+
+@pytest.mark.parametrize("d,k,margin", [(30, 10, 0), (30, 28, 16), (40, 40, 16), (64, 21, 16), (62, 5, 8)])
+def test_knn_list_lengths_and_unfolded_norms(gpu, d, k, margin):
+    """Every candidate-list length of the tensor-core kNN (16, 48, 64 slots)
+    and the dimensions above 61, where the reference norms are added in the
+    epilogue instead of folded into the MMA, against exact FP64 kNN, beside
+    a self-kNN of 9,220 rows, whose last reference split (of nine, 1,152 rows
+    each) holds four rows."""
+    from helpers import clustered_points
+    from scarf_gb300 import kernels as K
+    for n in (3000, 9220):
+        pts = clustered_points(n, d, seed=n + d)
+        ld = (d + 3) // 4 * 4
+        t = torch.zeros((n, ld), dtype=torch.float32, device="cuda")
+        t[:, :d] = torch.from_numpy(pts).cuda()
+        idx, dist, nm = K.knn(t, t, d, k, self_offset=0, margin=margin, precision="precision")
+        torch.cuda.synchronize()
+        gi = idx.cpu().numpy()
+        assert np.all((gi >= 0) & (gi < n))
+        _, od = oracle.exact_knn(pts, pts, k + 1)
+        assert oracle.recall_at_k(pts, pts, gi, od[:, -1]) >= 0.995
+        diff = pts[:, None, :].astype(np.float64) - pts[gi].astype(np.float64)
+        assert np.abs(dist.cpu().numpy() - (diff * diff).sum(-1)).max() <= 1e-4 * max(1.0, od.max())
