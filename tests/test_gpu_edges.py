@@ -130,3 +130,45 @@ def test_knn_list_lengths_and_unfolded_norms(gpu, d, k, margin):
         assert oracle.recall_at_k(pts, pts, gi, od[:, -1]) >= 0.995
         diff = pts[:, None, :].astype(np.float64) - pts[gi].astype(np.float64)
         assert np.abs(dist.cpu().numpy() - (diff * diff).sum(-1)).max() <= 1e-4 * max(1.0, od.max())
+
+
+def test_normalize_wide_output(gpu):
+    """More than 32,767 selected features: the column map stays int32 (the
+    narrow int16 map covers the usual widths) and each dense row buffer takes
+    most of a CTA's shared memory; values, library sizes and the column
+    statistics against the oracle."""
+    from scarf_gb300 import kernels as K
+    indptr, indices, data, G, _ = small_counts(n_cells=300, n_genes=42_000, seed=12)
+    feat = np.sort(np.random.default_rng(1).choice(G, 40_000, replace=False))
+    cmap = np.full(G, -1, np.int32)
+    cmap[feat] = np.arange(len(feat), dtype=np.int32)
+    h = len(feat)
+    cs = torch.zeros(h, dtype=torch.float64, device="cuda")
+    cq = torch.zeros_like(cs)
+    lib = torch.zeros(len(indptr) - 1, dtype=torch.int64, device="cuda")
+    x = K.normalize_csr(*(torch.from_numpy(a).cuda() for a in (indptr, indices, data, cmap)), h, colsum=cs,
+                        colsumsq=cq, libsize=lib)
+    torch.cuda.synchronize()
+    want, libw = oracle.normed_csr(indptr, indices, data, G, feat)
+    got = x[:, :h].double().cpu().numpy()
+    assert np.abs(got - want).max() <= 4e-7 * max(1.0, np.abs(want).max())
+    assert np.array_equal(lib.cpu().numpy(), np.asarray(libw).astype(np.int64))
+    assert np.allclose(cs.cpu().numpy(), want.sum(0), rtol=2e-6, atol=1e-6)
+    assert np.allclose(cq.cpu().numpy(), (want * want).sum(0), rtol=2e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("lc,bw", [(0.5, 1.5), (1.5, 1.0), (2.0, 2.5), (3.0, 1.5)])
+def test_smoothing_connectivity_and_bandwidth(gpu, lc, bw):
+    """make_graph's local_connectivity and bandwidth (rho interpolated between
+    non-zero distances, smooth_knn_dist's target log2(k) * bandwidth) against
+    the oracle, duplicates (zero distances) included."""
+    from helpers import clustered_points
+    from scarf_gb300 import kernels as K
+    pts = clustered_points(2000, 10, seed=31, dup=((1, 2), (3, 4), (3, 5)))
+    oi, od, _ = oracle.self_query_knn(pts, 11)
+    for chunk in (2000, 700):
+        edges, w = K.smooth(torch.from_numpy(oi.astype(np.int64)).cuda(), torch.from_numpy(od.astype(np.float32)).cuda(),
+                            lc, bw, chunk)
+        e, ow = oracle.smoothen_dists(oi, od, lc, bw, chunk)
+        assert np.array_equal(edges.cpu().numpy(), e.astype(np.int64))
+        assert np.abs(w.cpu().numpy() - ow).max() < 1e-5, (lc, bw, chunk)
