@@ -227,15 +227,17 @@ def make_graphs(samples, n_genes: int, feat_idx, dims: int = 30, k: int = 15, *,
     import concurrent.futures as cf
     dev = torch.device(device)
     out = [None] * len(samples)
+    import threading
     streams = [torch.cuda.Stream(dev) for _ in range(max(1, n_streams))]
     local = {}
+    lock = threading.Lock()
 
     def run(i):
-        import threading
         tid = threading.get_ident()
-        if tid not in local:
-            local[tid] = streams[len(local) % len(streams)]
-        st = local[tid]
+        with lock:              # each worker thread keeps one stream of its own
+            if tid not in local:
+                local[tid] = streams[len(local) % len(streams)]
+            st = local[tid]
         ip, ind, dat = samples[i]
         with torch.cuda.stream(st):
             g = make_graph(ip, ind, dat, n_genes, feat_idx, dims, k, precision=precision, device=dev, **kw)
