@@ -172,3 +172,54 @@ def test_smoothing_connectivity_and_bandwidth(gpu, lc, bw):
         e, ow = oracle.smoothen_dists(oi, od, lc, bw, chunk)
         assert np.array_equal(edges.cpu().numpy(), e.astype(np.int64))
         assert np.abs(w.cpu().numpy() - ow).max() < 1e-5, (lc, bw, chunk)
+
+
+@pytest.mark.parametrize("mix", [1.0, 0.5, 0.0])
+def test_union_mix_duplicates_self_loops_and_zeros(gpu, mix):
+    """The fuzzy union (umap.py:118-123, set_op_mix_ratio) of a graph with
+    repeated (row, column) pairs (summed, as the reference's CSR build does),
+    self loops and zero weights, bit for bit against scipy, zeros removed."""
+    from scarf_gb300 import kernels as K
+    rng = np.random.default_rng(2)
+    n, k = 500, 7
+    cols = rng.integers(0, n, size=(n, k))
+    cols[:, 3] = cols[:, 2]                      # the same neighbour twice in a row
+    cols[::7, 4] = np.arange(0, n, 7)            # self loops
+    w = rng.random(n * k).astype(np.float32).astype(np.float64)
+    w[::11] = 0.0                                # zero weights
+    edges = np.stack([np.repeat(np.arange(n), k), cols.ravel()], 1).astype(np.int64)
+    g = oracle.store_to_sparse(edges, w, n, k)
+    want = oracle.fuzzy_simplicial_set(g, mix).tocsr()
+    want.sort_indices()
+    ip, ind, dat = K.fuzzy_union(torch.from_numpy(edges).cuda(), torch.from_numpy(w).cuda(), n, k, mix=mix)
+    torch.cuda.synchronize()
+    assert np.array_equal(ip.cpu().numpy(), want.indptr)
+    assert np.array_equal(ind.cpu().numpy(), want.indices)
+    assert np.array_equal(dat.cpu().numpy(), want.data)
+
+
+def test_kmeans_one_centre_per_row(gpu):
+    """k = n = block rows: scikit-learn's k-means++ then picks every row, so
+    each row is its own centre and its own label."""
+    from scarf_gb300 import kernels as K
+    pts = np.random.default_rng(4).normal(size=(300, 12)).astype(np.float32)
+    x = torch.zeros((300, 12), dtype=torch.float32, device="cuda")
+    x[:] = torch.from_numpy(pts).cuda()
+    c, lab = K.kmeans(x, 12, 300, 300, 7)
+    torch.cuda.synchronize()
+    assert np.array_equal(lab.cpu().numpy(), np.arange(300))
+    assert np.array_equal(c.cpu().numpy(), pts.astype(np.float64))
+
+
+@pytest.mark.parametrize("k", [2, 3])
+def test_smoothing_few_neighbours(gpu, k):
+    """Very short rows (k = 2 and 3): the bisection sums from column 1 only."""
+    from helpers import clustered_points
+    from scarf_gb300 import kernels as K
+    pts = clustered_points(1200, 8, seed=5, dup=((1, 2),))
+    oi, od, _ = oracle.self_query_knn(pts, k)
+    edges, w = K.smooth(torch.from_numpy(oi.astype(np.int64)).cuda(), torch.from_numpy(od.astype(np.float32)).cuda(),
+                        1.0, 1.5, 500)
+    e, ow = oracle.smoothen_dists(oi, od, 1.0, 1.5, 500)
+    assert np.array_equal(edges.cpu().numpy(), e.astype(np.int64))
+    assert np.abs(w.cpu().numpy() - ow).max() < 1e-5
