@@ -223,3 +223,25 @@ def test_smoothing_few_neighbours(gpu, k):
     e, ow = oracle.smoothen_dists(oi, od, 1.0, 1.5, 500)
     assert np.array_equal(edges.cpu().numpy(), e.astype(np.int64))
     assert np.abs(w.cpu().numpy() - ow).max() < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["plain", "precision"])
+@pytest.mark.parametrize("nr", [12, 40, 129])
+def test_query_against_a_tiny_reference(gpu, precision, nr):
+    """Mapping queries (no self rule) against references fewer than a
+    candidate list's slots: every returned neighbour is a real reference."""
+    from helpers import clustered_points
+    from scarf_gb300 import kernels as K
+    refs = clustered_points(nr, 20, seed=nr)
+    q = clustered_points(700, 20, seed=nr + 1)
+    tr = torch.from_numpy(refs).cuda()
+    tq = torch.from_numpy(q).cuda()
+    k = min(11, nr)
+    idx, dist, _ = K.knn(tq, tr, 20, k, margin=16, precision=precision)
+    torch.cuda.synchronize()
+    gi = idx.cpu().numpy()
+    assert np.all((gi >= 0) & (gi < nr))
+    _, od = oracle.exact_knn(q, refs, k)
+    assert oracle.recall_at_k(q, refs, gi, od[:, -1]) >= 0.995
+    for row in gi:
+        assert len(set(row.tolist())) == k
