@@ -245,3 +245,30 @@ def test_query_against_a_tiny_reference(gpu, precision, nr):
     assert oracle.recall_at_k(q, refs, gi, od[:, -1]) >= 0.995
     for row in gi:
         assert len(set(row.tolist())) == k
+
+
+@pytest.mark.parametrize("h,dims", [(40, 20), (300, 64)])
+def test_projection_narrow_features_and_widest_basis(gpu, h, dims):
+    """The tensor-core projection with fewer features than one 64-feature
+    chunk (the rest of the box reads as zeros) and with the widest basis it
+    takes (64 scores), against the oracle's reducer; the plain form beside it."""
+    from scarf_gb300 import kernels as K
+    indptr, indices, data, G, _ = small_counts(n_cells=2000, n_genes=1500, seed=6)
+    feat = top_var_genes(indptr, indices, data, G, h)
+    cmap = np.full(G, -1, np.int32)
+    cmap[feat] = np.arange(h, dtype=np.int32)
+    cs = torch.zeros(h, dtype=torch.float64, device="cuda")
+    cq = torch.zeros_like(cs)
+    x = K.normalize_csr(*(torch.from_numpy(a).cuda() for a in (indptr, indices, data, cmap)), h, colsum=cs,
+                        colsumsq=cq)
+    mu, sg, mu32, sg32 = K.zstats(cs, cq, x.shape[0])
+    cov, zsum = K.covariance(x, mu32, sg32, n_cols=h)
+    comps, _, _, l32 = K.pca_basis(cov, zsum, x.shape[0], dims + 1, n_load=dims, ld_l=dims)
+    xw, _ = oracle.normed_csr(indptr, indices, data, G, feat)
+    omu, osg = oracle.zstats(xw)
+    want = oracle.reducer(xw, omu, osg, comps.cpu().numpy()[:, :dims])
+    for form, tol in (("plain", 2e-5), ("precision", 1e-4)):
+        s = K.project(x, mu32, sg32, l32, dims, n_cols=h, ld_s=(dims + 3) // 4 * 4, precision=form)
+        torch.cuda.synchronize()
+        got = s[:, :dims].cpu().numpy()
+        assert np.abs(got - want).max() <= tol * max(1.0, np.abs(want).max()), form
