@@ -272,6 +272,35 @@ __device__ __forceinline__ void warp_bitonic_sort(unsigned long long (&v)[SLOTS]
 // candidates lane + 32 s, the warp sorts the keys, and every lane writes its
 // own output positions; the self rule uses ballots. The same keys in the same
 // total order as the list merge below, so the same output.
+// Exact FP32 sum over c < d of (q[c] - r[c])^2, accumulated in the order
+// c = 0 .. d-1; the reference row is read 16 bytes at a time when its rows are
+// 16-byte aligned (each lane reads its own candidate row, so wide loads cut
+// the L1 wavefronts of the gather by four).
+__device__ __forceinline__ float rerank_dist(const float* __restrict__ qv, const float* __restrict__ r, int d,
+                                             bool vec) {
+  float acc = 0.f;
+  int c = 0;
+  if (vec) {
+    const float4* r4 = reinterpret_cast<const float4*>(r);
+    for (; c + 3 < d; c += 4) {
+      const float4 v = __ldg(r4 + (c >> 2));
+      float df = qv[c] - v.x;
+      acc = fmaf(df, df, acc);
+      df = qv[c + 1] - v.y;
+      acc = fmaf(df, df, acc);
+      df = qv[c + 2] - v.z;
+      acc = fmaf(df, df, acc);
+      df = qv[c + 3] - v.w;
+      acc = fmaf(df, df, acc);
+    }
+  }
+  for (; c < d; ++c) {
+    const float df = qv[c] - __ldg(r + c);
+    acc = fmaf(df, df, acc);
+  }
+  return acc;
+}
+
 template <int SLOTS>
 __global__ void __launch_bounds__(128)
 rerank_sort_kernel(const float* __restrict__ queries, const float* __restrict__ refs, int d, int ld, int64_t nq,
@@ -284,6 +313,7 @@ rerank_sort_kernel(const float* __restrict__ queries, const float* __restrict__ 
   if (q >= nq) return;  // whole warps
   for (int c = lane; c < d; c += 32) qs[warp][c] = queries[q * ld + c];
   __syncwarp();
+  const bool vec = (ld & 3) == 0 && (reinterpret_cast<uintptr_t>(refs) & 15) == 0;
   const int total = nlists * kc;
   unsigned long long v[SLOTS];
 #pragma unroll
@@ -293,12 +323,7 @@ rerank_sort_kernel(const float* __restrict__ queries, const float* __restrict__ 
     if (e >= total) continue;
     const int ci = cand[(int64_t(e / kc) * nq_pad + q) * kc + e % kc];
     if (ci < 0) continue;
-    const float* r = refs + int64_t(ci) * ld;
-    float acc = 0.f;
-    for (int c = 0; c < d; ++c) {
-      const float df = qs[warp][c] - __ldg(r + c);
-      acc = fmaf(df, df, acc);
-    }
+    const float acc = rerank_dist(qs[warp], refs + int64_t(ci) * ld, d, vec);
     v[s] = (static_cast<unsigned long long>(__float_as_uint(acc)) << 32) | unsigned(ci);
   }
   warp_bitonic_sort<SLOTS>(v, lane);
@@ -354,12 +379,7 @@ rerank_kernel(const float* __restrict__ queries, const float* __restrict__ refs,
     const int l = e / kc, j = e % kc;
     const int ci = cand[(int64_t(l) * nq_pad + q) * kc + j];
     if (ci < 0) continue;
-    const float* r = refs + int64_t(ci) * ld;
-    float s = 0.f;
-    for (int c = 0; c < d; ++c) {
-      const float df = qs[warp][c] - __ldg(r + c);
-      s = fmaf(df, df, s);
-    }
+    const float s = rerank_dist(qs[warp], refs + int64_t(ci) * ld, d, false);
     const unsigned long long key = (static_cast<unsigned long long>(__float_as_uint(s)) << 32) | unsigned(ci);
     if (key < top.worst()) top.insert(key);
   }
