@@ -1,16 +1,18 @@
 #!/usr/bin/env python
 """make_graph throughput of scarf's graph-construction path on GB300.
 
-Workload (default, ``--config c2``): 100,000 cells x 30,000 genes of seeded
-negative-binomial counts (20 clusters), 2,000 HVGs, 50 PCs, k = 21, smoothing
-chunks of 1,000 rows. One step = normalise -> z-stats -> scatter -> FP64 eigh
--> projection -> self-kNN (+ self removal) -> smoothing over the whole matrix.
+Workload (default, ``--config c3``): 1,000,000 cells x 30,000 genes of seeded
+negative-binomial counts (40 clusters), 2,000 HVGs, 50 PCs, k = 21, smoothing
+chunks of 1,000 rows (``--config c2``: 100,000 cells, 20 clusters). One step =
+normalise -> z-stats -> scatter -> FP64 eigh -> projection -> self-kNN (+ self
+removal) -> smoothing over the whole matrix.
 
 * ``value``: cells/s of the precision form (BF16 tcgen05 distances + FP32
   re-rank of k+1+16 candidates) with the CSR already resident in HBM.
 * ``e2e``: the same through the public pipeline call with pinned HOST CSR,
-  host->device copies and the device->host read of indices, distances, edges
-  and weights inside every timed step.
+  which the normalisation kernel reads over the host link in 50,000-cell
+  chunks, and the device->host read of indices, distances, edges and weights
+  inside every timed step.
 * ``plain``: the all-FP32 form on the same input.
 * ``--impl reference``: the CPU restatement of the reference path (the
   oracle), timed on a bounded sample of the same workload on the host cores.
@@ -518,6 +520,17 @@ def run_gb300(args, cfg):
     d2h = int(sum(v.numel() * v.element_size() for v in outs.values()))
     del outs, res_h
     link = host_link(dev)
+    # the normalisation reading the pinned CSR over the link itself (the e2e form)
+    zc = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        pipeline.normalize_csr_host(ip_h, ind_h, dat_h, G, feat, chunk_cells=chunk, device=dev)
+        e1.record()
+        e1.synchronize()
+        zc.append(e0.elapsed_time(e1))
+    link["normalize_read_gbs"] = round(h2d / (min(zc) * 1e-3) / 1e9, 1)
+    link["normalize_read_ms"] = round(min(zc), 3)
     # the step cannot beat the larger of its device time and its copies at the link's rate
     bound_ms = max(ms, h2d / (link["h2d_gbs"] * 1e9) * 1e3 + d2h / (link["d2h_gbs"] * 1e9) * 1e3)
     ds_e2e = None if args.no_datastore else datastore_e2e(csr, feat, cfg)
@@ -566,8 +579,9 @@ def run_gb300(args, cfg):
         "e2e": {"value": round(cells / (e2e_ms * 1e-3), 1), "unit": "cells/s", "ms_per_step": round(e2e_ms, 3),
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "host_link": link,
                 "bound_ms": round(bound_ms, 3), "frac_of_bound": round(bound_ms / e2e_ms, 4),
-                "call": "pipeline.make_graph on pinned host CSR (chunks of %s cells), outputs read back"
-                        % (chunk or "8ths of the"), "clocks": clocks_e2e},
+                "call": "pipeline.make_graph on pinned host CSR, read over the host link by the normalisation "
+                        "kernel itself (%s), outputs read back"
+                        % ("chunks of %d cells" % chunk if chunk else "one launch"), "clocks": clocks_e2e},
         "e2e_datastore": ds_e2e,
         "serving": serving,
         "roofline": roof,

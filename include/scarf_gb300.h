@@ -108,7 +108,11 @@ int sg_profile_query(sg_handle* h, const char* name, double* total_ms, long long
  *   take fill_value instead (mapping_utils.py:208 fills 1.0); missing_mask may
  *   be NULL. libsize_out[n_rows] (int64, may be NULL) receives s_r for the
  *   renormalised form. colsum/colsumsq (n_cols doubles, may be NULL) are
- *   ACCUMULATED with the sums of the written values, in a fixed order. */
+ *   ACCUMULATED with the sums of the written values, in a fixed order.
+ *   indptr/indices/data may be device memory or page-locked host memory
+ *   (cudaHostAlloc / cudaHostRegister): the kernel then reads the rows over
+ *   the host link itself, with no staging copy. Pageable host memory is
+ *   refused with SG_ERR_ARG. */
 int sg_normalize_csr(sg_handle* h, const int64_t* indptr, const int32_t* indices,
                      const int32_t* data, int64_t n_rows, const int32_t* col_map,
                      int64_t n_genes, int32_t n_cols, const uint8_t* missing_mask,

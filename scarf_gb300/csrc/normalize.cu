@@ -10,6 +10,9 @@
 // run to run. Per-CTA partials are reduced in FP64 in a fixed order.
 #include "common.cuh"
 
+#include <initializer_list>
+#include <utility>
+
 namespace {
 
 constexpr int kRounds = 8;  // rows per warp per CTA
@@ -332,6 +335,33 @@ __global__ void zstats_kernel(const double* __restrict__ colsum, const double* _
   if (sigma32) sigma32[j] = float(sd);
 }
 
+// A CSR array the kernels may read: device memory of this handle's device,
+// managed memory, or page-locked host memory mapped at the same address
+// (read over the host link). Pageable host memory is refused.
+int check_readable(const sg_handle* h, const void* p, const char* what) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return sg::fail(SG_ERR_ARG, "sg_normalize_csr: %s is not a CUDA-visible pointer", what);
+  }
+  switch (a.type) {
+    case cudaMemoryTypeDevice:
+      if (a.device != h->device)
+        return sg::fail(SG_ERR_ARG, "sg_normalize_csr: %s lives on device %d, the handle on %d", what, a.device,
+                        h->device);
+      return SG_OK;
+    case cudaMemoryTypeManaged:
+      return SG_OK;
+    case cudaMemoryTypeHost:
+      if (a.devicePointer != p)
+        return sg::fail(SG_ERR_ARG, "sg_normalize_csr: page-locked %s is not mapped at its host address", what);
+      return SG_OK;
+    default:
+      return sg::fail(SG_ERR_ARG, "sg_normalize_csr: %s is pageable host memory (pass device or page-locked memory)",
+                      what);
+  }
+}
+
 }  // namespace
 
 extern "C" int sg_normalize_csr(sg_handle* h, const int64_t* indptr, const int32_t* indices,
@@ -358,6 +388,12 @@ extern "C" int sg_normalize_csr(sg_handle* h, const int64_t* indptr, const int32
            "sg_normalize_csr: bf16 output needs an even ld_out and 4-byte alignment");
   if (n_rows == 0) return SG_OK;
   SG_ARG(indices && data, "sg_normalize_csr: null indices/data");
+  for (const auto& pa : {std::make_pair(static_cast<const void*>(indptr), "indptr"),
+                         std::make_pair(static_cast<const void*>(indices), "indices"),
+                         std::make_pair(static_cast<const void*>(data), "data")}) {
+    const int rc = check_readable(h, pa.first, pa.second);
+    if (rc) return rc;
+  }
 
   const int pitch = (n_cols + 3) & ~3;
   const size_t row_bytes = size_t(pitch) * sizeof(float);

@@ -24,6 +24,7 @@ from . import kernels as K
 from .ann import AnnStream, GpuExactIndex, NormalizedData
 from .knn_utils import self_query_knn, smoothen_dists
 from .pipeline import col_map as _col_map
+from .pipeline import normalize_csr_host
 from .store import Group, create_zarr_dataset
 
 log = logging.getLogger("scarf_gb300")
@@ -106,9 +107,16 @@ class RNAassay:
     def __init__(self, name: str, indptr, indices, data, n_genes: int, cells: MetaData, feats: MetaData,
                  z: Group, device="cuda"):
         self.name = name
-        self.indptr = np.asarray(indptr, dtype=np.int64)
-        self.indices = np.asarray(indices, dtype=np.int32)
-        self.data = np.asarray(data, dtype=np.int32)
+        ip = np.ascontiguousarray(indptr, dtype=np.int64)
+        ind = np.ascontiguousarray(indices, dtype=np.int32)
+        dat = np.ascontiguousarray(data, dtype=np.int32)
+        self._pinned = None
+        if torch.device(device).type == "cuda" and torch.cuda.is_available() and len(ind):
+            # page-locked copies, which the normalisation kernel reads over the
+            # host link itself (no staging copy of the counts on the device)
+            self._pinned = [torch.from_numpy(a).pin_memory() for a in (ip, ind, dat)]
+            ip, ind, dat = (t.numpy() for t in self._pinned)
+        self.indptr, self.indices, self.data = ip, ind, dat
         self.n_genes = int(n_genes)
         self.cells = cells
         self.feats = feats
@@ -147,16 +155,16 @@ class RNAassay:
             log.info(f"Using existing normalized data with cell key {cell_key} and feat key {feat_key}")
             return self._normed_cache[ck]
         g = self.z.create_group(location, overwrite=True)
-        ip, ind, dat = self._rows(cell_idx)
         h = len(feat_idx)
         dev = self.device
-        nc = None if renormalize_subset else torch.from_numpy(self.n_counts()[cell_idx]).to(dev)
-        x = torch.empty((len(ip) - 1, K.round_up(h, 4)), dtype=torch.float32, device=dev)
-        cs = torch.zeros(h, dtype=torch.float64, device=dev)
-        cq = torch.zeros_like(cs)
-        K.normalize_csr(torch.from_numpy(ip).to(dev), torch.from_numpy(ind).to(dev), torch.from_numpy(dat).to(dev),
-                        _col_map(feat_idx, self.n_genes, dev), h, size_factor=self.sf, log_transform=log_transform,
-                        renormalize_subset=renormalize_subset, n_counts=nc, out=x, colsum=cs, colsumsq=cq)
+        if self._pinned is not None and len(cell_idx) == len(self.indptr) - 1:
+            rows = self._pinned     # read in place over the host link
+        else:
+            rows = [torch.from_numpy(a) for a in self._rows(cell_idx)]   # one copy to the device
+        nc = None if renormalize_subset else self.n_counts()[cell_idx]
+        x, cs, cq = normalize_csr_host(*rows, self.n_genes, feat_idx, size_factor=self.sf,
+                                       log_transform=log_transform, renormalize_subset=renormalize_subset,
+                                       n_counts=nc, chunk_cells=0, device=dev)
         nd = NormalizedData(x, h, batch_size)
         nd.colsum, nd.colsumsq = cs, cq
         if persist_normed:

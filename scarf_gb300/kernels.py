@@ -78,9 +78,11 @@ def _stream(device) -> C.c_void_p:
     return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
 
 
-def _need(t: torch.Tensor, name: str, dtype=None, ndim=None, contiguous=True):
-    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+def _need(t: torch.Tensor, name: str, dtype=None, ndim=None, contiguous=True, pinned_ok=False):
+    if not isinstance(t, torch.Tensor):
         raise TypeError(f"{name} must be a CUDA tensor")
+    if not t.is_cuda and not (pinned_ok and t.device.type == "cpu" and t.is_pinned()):
+        raise TypeError(f"{name} must be a CUDA tensor" + (" or page-locked host tensor" if pinned_ok else ""))
     if dtype is not None and t.dtype != dtype:
         raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
     if ndim is not None and t.dim() != ndim:
@@ -97,14 +99,17 @@ def round_up(x: int, m: int) -> int:
 def normalize_csr(indptr, indices, data, col_map, n_cols: int, *, size_factor: float = 1000.0,
                   log_transform: bool = True, renormalize_subset: bool = True, n_counts=None,
                   missing_mask=None, fill_value: float = 1.0, out=None, out_dtype=torch.float32,
-                  colsum=None, colsumsq=None, libsize=None) -> torch.Tensor:
-    """a1: dense normalised rows (n_rows x ld) from CSR counts; see sg_normalize_csr."""
-    _need(indptr, "indptr", torch.int64, 1)
-    _need(indices, "indices", torch.int32, 1)
-    _need(data, "data", torch.int32, 1)
+                  colsum=None, colsumsq=None, libsize=None, device=None) -> torch.Tensor:
+    """a1: dense normalised rows (n_rows x ld) from CSR counts; see sg_normalize_csr.
+    indptr/indices/data may be CUDA tensors or page-locked host tensors, which
+    the kernel reads over the host link (``device`` then names the GPU; by
+    default that of ``col_map``)."""
+    _need(indptr, "indptr", torch.int64, 1, pinned_ok=True)
+    _need(indices, "indices", torch.int32, 1, pinned_ok=True)
+    _need(data, "data", torch.int32, 1, pinned_ok=True)
     _need(col_map, "col_map", torch.int32, 1)
     n_rows = indptr.numel() - 1
-    dev = indptr.device
+    dev = col_map.device if device is None else torch.device(device)
     if out is None:
         ld = round_up(n_cols, 4 if out_dtype == torch.float32 else 8)
         out = torch.empty((n_rows, ld), dtype=out_dtype, device=dev)

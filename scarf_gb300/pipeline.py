@@ -2,9 +2,10 @@
 
 normalise (+ column sums) -> z-statistics -> scatter -> FP64 eigh -> projection
 -> exact self-kNN (+ self removal, recall) -> smoothing, all resident in HBM.
-The CSR may be given as host arrays (copied in, optionally streamed in chunks
-of cells from pinned memory with the copy of chunk i+1 overlapping the
-normalisation of chunk i) or as CUDA tensors.
+The CSR may be given as CUDA tensors, as page-locked host tensors (which the
+normalisation kernel reads over the host link itself, with no staging copy)
+or as other host arrays (copied in chunks of cells, the copy of chunk i+1
+overlapping the normalisation of chunk i).
 
 Step order and parameters follow DataStore.make_graph
 (scarf/datastore/graph_datastore.py:513-1020).
@@ -77,11 +78,14 @@ def col_map(feat_idx, n_genes: int, device) -> torch.Tensor:
 def normalize_csr_host(indptr, indices, data, n_genes: int, feat_idx, *, size_factor=1000.0,
                        log_transform=True, renormalize_subset=True, n_counts=None, chunk_cells=None,
                        device="cuda", missing_mask=None, fill_value=1.0, cmap=None):
-    """a1+a3 over host (ideally pinned) CSR arrays. With ``chunk_cells`` the rows
-    are streamed: chunk i+1 is copied on a side stream while chunk i is
-    normalised. Host inputs are streamed in about 8 chunks unless
-    ``chunk_cells`` says otherwise (0: one copy); chunks are whole multiples
-    of the 256-row statistics slices. Returns ``(x, colsum, colsumsq)``."""
+    """a1+a3 over host CSR arrays. Page-locked (pinned) ``indices`` and
+    ``data`` tensors are read by the row kernel over the host link, with no
+    staging copy and no device copy of the CSR: one launch, or one per
+    ``chunk_cells`` rows. Other host arrays are streamed through device
+    staging slots: chunk i+1 is copied on a side stream while chunk i is
+    normalised, in about 8 chunks unless ``chunk_cells`` says otherwise (0:
+    one copy). Chunks are whole multiples of the 256-row statistics slices,
+    so every form gives the same bits. Returns ``(x, colsum, colsumsq)``."""
     dev = torch.device(device)
     h = len(feat_idx)
     n = len(indptr) - 1
@@ -99,12 +103,28 @@ def normalize_csr_host(indptr, indices, data, n_genes: int, feat_idx, *, size_fa
         ind_h = ind_h.to(torch.int32)
     if dat_h.dtype != torch.int32:
         dat_h = dat_h.to(torch.int32)
-    if chunk_cells is None and ind_h.device.type == "cpu":
+    host = ind_h.device.type == "cpu"
+    pinned = host and ind_h.numel() > 0 and ind_h.is_pinned() and dat_h.is_pinned()
+    if chunk_cells is None and host and not pinned:
         chunk_cells = max(16384, -(-n // 8))
     if chunk_cells:
         # whole slices of the column-statistics pass (256 rows): the streamed
         # sums then add the same FP32 slice partials as one pass over all rows
         chunk_cells = -(-int(chunk_cells) // STAT_ROWS) * STAT_ROWS
+    if pinned:
+        ipn = ip_h.numpy() if ip_h.device.type == "cpu" else ip_h.cpu().numpy()
+        ip_r = ip_h if (ip_h.device.type == "cpu" and ip_h.is_pinned()) or ip_h.is_cuda else ip_h.to(dev)
+        bounds = [0, n] if not chunk_cells or chunk_cells >= n else list(range(0, n, chunk_cells)) + [n]
+        last = ind_h.numel() - 1
+        for a, b in zip(bounds[:-1], bounds[1:]):
+            # the chunk's entries start at indptr[a]; a chunk of empty rows at
+            # the very end reads nothing, so any entry address serves it
+            off = min(int(ipn[a] - ipn[0]), last)
+            K.normalize_csr(ip_r[a:b + 1], ind_h[off:], dat_h[off:], cmap, h, size_factor=size_factor,
+                            log_transform=log_transform, renormalize_subset=renormalize_subset,
+                            n_counts=None if nc is None else nc[a:b], missing_mask=mm, fill_value=fill_value,
+                            out=x[a:b], colsum=cs, colsumsq=cq, device=dev)
+        return x, cs, cq
     if not chunk_cells or chunk_cells >= n:
         ip = ip_h.to(dev, non_blocking=True)
         ind = ind_h.to(dev, non_blocking=True)
@@ -132,7 +152,7 @@ def normalize_csr_host(indptr, indices, data, n_genes: int, feat_idx, *, size_fa
 
     def stage(ci):
         a, b = bounds[ci], bounds[ci + 1]
-        pa, pb = int(ipn[a]), int(ipn[b])
+        pa, pb = int(ipn[a] - ipn[0]), int(ipn[b] - ipn[0])
         sl = ci % nslot
         t_ip, t_ind, t_dat = slots[sl]
         with torch.cuda.stream(side):
@@ -149,7 +169,7 @@ def normalize_csr_host(indptr, indices, data, n_genes: int, feat_idx, *, size_fa
         stage(ci)
     for ci in range(nch):
         a, b = bounds[ci], bounds[ci + 1]
-        pa, pb = int(ipn[a]), int(ipn[b])
+        pa, pb = int(ipn[a] - ipn[0]), int(ipn[b] - ipn[0])
         sl = ci % nslot
         t_ip, t_ind, t_dat = slots[sl]
         comp.wait_event(landed[ci])

@@ -192,21 +192,61 @@ def test_make_graph_writes_kmeans_and_run_umap(ds):
 
 
 def test_streamed_host_csr_equals_device_csr():
-    """Host CSR streamed in chunks through the three-slot staging ring (the
-    copy of chunk i+1 overlapping the normalisation of chunk i, ragged last
-    chunk, an empty row) gives the graph of the same CSR on the device: the
-    chunks are whole 256-row slices of the column statistics, so only the FP64
-    order of adding the slice partials differs."""
+    """Host CSR gives the graph of the same CSR on the device, in every form:
+    page-locked arrays read by the row kernel over the host link (one launch,
+    or one per chunk; indptr pinned or not), and pageable arrays streamed in
+    chunks through the three-slot staging ring (the copy of chunk i+1
+    overlapping the normalisation of chunk i). Ragged last chunk, an empty
+    row. The chunks are whole 256-row slices of the column statistics, so only
+    the FP64 order of adding the slice partials differs."""
     from scarf_gb300 import pipeline
     indptr, indices, data, G, _ = small_counts(n_cells=2300, seed=5)
     feat = top_var_genes(indptr, indices, data, G, 300)
     pin = [torch.from_numpy(a).pin_memory() for a in (indptr, indices, data)]
+    pageable = [torch.from_numpy(a.copy()) for a in (indptr, indices, data)]
+    mixed = [pageable[0], pin[1], pin[2]]
     dev = [t.cuda() for t in pin]
     b = pipeline.make_graph(*dev, G, feat, 20, 10, precision="precision")
-    for chunk in (500, 777, 2300):
-        a = pipeline.make_graph(*pin, G, feat, 20, 10, precision="precision", chunk_cells=chunk)
+    for arrays, chunks in ((pin, (None, 500, 777, 2300)), (mixed, (None, 1000)), (pageable, (500, 777, None))):
+        for chunk in chunks:
+            a = pipeline.make_graph(*arrays, G, feat, 20, 10, precision="precision", chunk_cells=chunk)
+            torch.cuda.synchronize()
+            assert torch.equal(a.x, b.x)
+            assert torch.allclose(a.mu, b.mu, rtol=1e-14, atol=0)
+            assert torch.allclose(a.sigma, b.sigma, rtol=1e-14, atol=0)
+            assert torch.equal(a.mu32, b.mu32) and torch.equal(a.sigma32, b.sigma32)
+            assert torch.equal(a.indices, b.indices) and torch.equal(a.weights, b.weights)
+
+
+def test_pinned_csr_trailing_empty_rows_and_pageable_refusal():
+    """Page-locked CSR whose last chunk holds only empty rows, and a CSR that
+    starts at a non-zero indptr[0], normalise like the device copy; the C ABI
+    refuses pageable host pointers before any launch."""
+    from scarf_gb300 import _lib as L
+    from scarf_gb300 import kernels as K
+    from scarf_gb300 import pipeline
+    indptr, indices, data, G, _ = small_counts(n_cells=1000, seed=9)
+    n = len(indptr) - 1
+    feat = top_var_genes(indptr, indices, data, G, 200)
+    indptr = np.concatenate([indptr, np.full(600, indptr[-1], dtype=indptr.dtype)])  # 600 empty rows
+    ip = torch.from_numpy(indptr).pin_memory()
+    ind, dat = torch.from_numpy(indices).pin_memory(), torch.from_numpy(data).pin_memory()
+    xd, sd, qd = pipeline.normalize_csr_host(ip.cuda(), ind.cuda(), dat.cuda(), G, feat)
+    for chunk in (None, 512, 256):
+        x, s, q = pipeline.normalize_csr_host(ip, ind, dat, G, feat, chunk_cells=chunk)
         torch.cuda.synchronize()
-        assert torch.equal(a.x, b.x)
-        assert torch.allclose(a.mu, b.mu, rtol=1e-14, atol=0) and torch.allclose(a.sigma, b.sigma, rtol=1e-14, atol=0)
-        assert torch.equal(a.mu32, b.mu32) and torch.equal(a.sigma32, b.sigma32)
-        assert torch.equal(a.indices, b.indices) and torch.equal(a.weights, b.weights)
+        assert torch.equal(x, xd) and torch.allclose(s, sd, rtol=1e-14, atol=0)
+    assert torch.count_nonzero(x[n:]) == 0
+    # rows 300.. on their own: indptr starts at indptr[300], the entries at that offset
+    a = 300
+    off = int(indptr[a])
+    x2, _, _ = pipeline.normalize_csr_host(ip[a:], ind[off:], dat[off:], G, feat)
+    torch.cuda.synchronize()
+    assert torch.equal(x2, xd[a:])
+    cmap = pipeline.col_map(feat, G, "cuda")
+    out = torch.empty((n, K.round_up(len(feat), 4)), dtype=torch.float32, device="cuda")
+    with pytest.raises(ValueError, match="pageable"):
+        L.check(L.load().sg_normalize_csr(
+            K.handle(0).ptr, indptr.ctypes.data, indices.ctypes.data, data.ctypes.data, n, cmap.data_ptr(), G,
+            len(feat), None, 1.0, None, 1000.0, L.SG_NORM_LOG1P | L.SG_NORM_RENORM_SUBSET, out.data_ptr(),
+            out.stride(0), L.SG_F32, None, None, None, None))
