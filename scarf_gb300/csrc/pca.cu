@@ -780,6 +780,19 @@ struct FilterBufs {
   int* info;  // one slot per factorisation
   int n_info;
   int cap_info;
+  syevjInfo_t jac = nullptr;  // Jacobi settings for blocks of up to kJacobiMax columns
+};
+
+// Blocks up to this width take cuSOLVER's Jacobi eigensolver in the FP32
+// Rayleigh-Ritz step (1.56 against 1.98 ms at 128 on a GB300; at 192 the
+// divide-and-conquer solver is faster, 1.55 against 2.7 ms).
+constexpr int kJacobiMax = 128;
+
+struct JacobiGuard {
+  syevjInfo_t p = nullptr;
+  ~JacobiGuard() {
+    if (p) cusolverDnDestroySyevjInfo(p);
+  }
 };
 
 // Y <- Y D L^-T with (Y D)^T (Y D) = L L^T and D the column scaling, in place
@@ -872,8 +885,13 @@ int ritz_f32(sg_handle* h, cusolverDnHandle_t sol, cublasHandle_t blas, const fl
   SG_BLAS(cublasSgemm(blas, CUBLAS_OP_T, CUBLAS_OP_N, m, m, n, &one, b.X, n, b.P, n, &zero, b.G, m));
   int* inf = b.info + std::min(b.n_info, b.cap_info - 1);
   ++b.n_info;
-  SG_SOLVER(cusolverDnSsyevd(sol, vectors ? CUSOLVER_EIG_MODE_VECTOR : CUSOLVER_EIG_MODE_NOVECTOR,
-                             CUBLAS_FILL_MODE_LOWER, m, b.G, m, b.W, static_cast<float*>(h->solver_work), lwork_s, inf));
+  const cusolverEigMode_t mode = vectors ? CUSOLVER_EIG_MODE_VECTOR : CUSOLVER_EIG_MODE_NOVECTOR;
+  if (b.jac && m <= kJacobiMax)
+    SG_SOLVER(cusolverDnSsyevj(sol, mode, CUBLAS_FILL_MODE_LOWER, m, b.G, m, b.W, static_cast<float*>(h->solver_work),
+                               int(h->solver_work_bytes / sizeof(float)), inf, b.jac));
+  else
+    SG_SOLVER(cusolverDnSsyevd(sol, mode, CUBLAS_FILL_MODE_LOWER, m, b.G, m, b.W, static_cast<float*>(h->solver_work),
+                               lwork_s, inf));
   if (vectors) {
     reverse_cols_kernel<<<sg::ceil_div_i(int64_t(m / 2) * m, 256), 256, 0, st>>>(b.G, m);
     SG_LAUNCH_CHECK();
@@ -984,6 +1002,17 @@ extern "C" int sg_pca_basis_filter(sg_handle* h, const double* cov, const double
   int lw_potrf = 0, lw_s = 0, lw_d = 0, lw_dp = 0;
   SG_SOLVER(cusolverDnSpotrf_bufferSize(sol, CUBLAS_FILL_MODE_LOWER, m, b.G, m, &lw_potrf));
   SG_SOLVER(cusolverDnSsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, b.G, m, b.W, &lw_s));
+  JacobiGuard jac;
+  if (m <= kJacobiMax) {
+    SG_SOLVER(cusolverDnCreateSyevjInfo(&jac.p));
+    SG_SOLVER(cusolverDnXsyevjSetTolerance(jac.p, 0.0));   // machine accuracy
+    SG_SOLVER(cusolverDnXsyevjSetMaxSweeps(jac.p, 20));
+    int lw_j = 0;
+    SG_SOLVER(cusolverDnSsyevj_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, m, b.G, m, b.W,
+                                          &lw_j, jac.p));
+    lw_s = std::max(lw_s, lw_j);
+    b.jac = jac.p;
+  }
   SG_SOLVER(cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, p, Bd, p, Wd, &lw_d));
   SG_SOLVER(cusolverDnDpotrf_bufferSize(sol, CUBLAS_FILL_MODE_LOWER, p, Gd, p, &lw_dp));
   const size_t wb = std::max(std::max(sizeof(float) * size_t(lw_potrf), sizeof(float) * size_t(lw_s)),
