@@ -54,45 +54,87 @@ __device__ __forceinline__ float zero_shift(float mu, float sg) {
   return z0 - __bfloat162float(__float2bfloat16_rn(z0));
 }
 
+constexpr int ZR = 128;  // cells per zsplit tile
+
+// z' = (x - mu)/sigma - delta for a tile of 128 cells x 64 features: the rows
+// read 16 lanes per row (16-byte vectors when kVec: rows 16-byte aligned),
+// the column sums of z per 64-cell half in row order (the partials of 64-row
+// tiles), and the transposed hi/lo values written two cells per lane (128 B
+// per warp store, 256 B per feature and tile).
+template <bool kVec>
 __global__ void __launch_bounds__(256)
 zsplit_kernel(const float* __restrict__ x, int64_t n_rows, int n_cols, int64_t ld, const float* __restrict__ mu,
               const float* __restrict__ sg, const uint8_t* __restrict__ mask, __nv_bfloat16* __restrict__ hi,
               __nv_bfloat16* __restrict__ lo, int64_t n_pad, float* __restrict__ zpart, int h_pad) {
-  __shared__ float t[ZT][ZT + 1];
-  __shared__ float dl[ZT];
-  __shared__ uint8_t valid[ZT];
-  const int64_t r0 = int64_t(blockIdx.x) * ZT;
+  __shared__ float t[ZR][ZT + 1];
+  __shared__ float smu[ZT], ssg[ZT], dl[ZT];
+  __shared__ uint8_t valid[ZR];
+  const int64_t r0 = int64_t(blockIdx.x) * ZR;
   const int c0 = blockIdx.y * ZT;
-  const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;  // 64 x 4
-  if (threadIdx.x < ZT) {
-    const int c = c0 + threadIdx.x;
-    dl[threadIdx.x] = c < n_cols ? zero_shift(mu[c], sg[c]) : 0.f;
-    const int64_t r = r0 + threadIdx.x;
-    valid[threadIdx.x] = (r < n_rows && (mask == nullptr || mask[r] != 0)) ? 1 : 0;
+  const int tid = threadIdx.x;
+  if (tid < ZT) {
+    const int c = c0 + tid;
+    smu[tid] = c < n_cols ? mu[c] : 0.f;
+    ssg[tid] = c < n_cols ? sg[c] : 1.f;
+    dl[tid] = c < n_cols ? zero_shift(mu[c], sg[c]) : 0.f;
+  }
+  if (tid < ZR) {
+    const int64_t r = r0 + tid;
+    valid[tid] = (r < n_rows && (mask == nullptr || mask[r] != 0)) ? 1 : 0;
   }
   __syncthreads();
-  for (int rr = ty; rr < ZT; rr += 4) {
-    const int64_t r = r0 + rr;
-    const int c = c0 + tx;
-    float z = 0.f;
-    if (valid[rr] && c < n_cols) z = __fdiv_rn(x[r * ld + c] - mu[c], sg[c]);
-    t[rr][tx] = z;
+  // 128 rows x 16 groups of 4 features: 8 per thread, 16 lanes per row
+#pragma unroll
+  for (int i = 0; i < (ZR * ZT / 4) / 256; ++i) {
+    const int task = tid + 256 * i;
+    const int rr = task >> 4, g = task & 15;
+    const int c = c0 + 4 * g;
+    float e4[4] = {0.f, 0.f, 0.f, 0.f};
+    if (valid[rr] && c < n_cols) {
+      const float* src = x + (r0 + rr) * ld + c;
+      if (kVec) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(src));
+        e4[0] = v.x;
+        e4[1] = v.y;
+        e4[2] = v.z;
+        e4[3] = v.w;
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (c + e < n_cols) e4[e] = __ldg(src + e);
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int cc = 4 * g + e;
+      t[rr][cc] = (valid[rr] && c + e < n_cols) ? __fdiv_rn(e4[e] - smu[cc], ssg[cc]) : 0.f;
+    }
   }
   __syncthreads();
-  // column sums of z over this row tile
-  if (threadIdx.x < ZT) {
-    float s = 0.f;
-    for (int rr = 0; rr < ZT; ++rr) s += t[rr][threadIdx.x];
-    zpart[int64_t(blockIdx.x) * h_pad + c0 + threadIdx.x] = s;
+  // column sums of z over each 64-row half, rows in order
+  if (tid < 2 * ZT) {
+    const int c = tid & (ZT - 1), hh = tid >> 6;
+    if (r0 + hh * ZT < n_pad) {
+      float s = 0.f;
+      for (int rr = 0; rr < ZT; ++rr) s += t[hh * ZT + rr][c];
+      zpart[(int64_t(blockIdx.x) * 2 + hh) * h_pad + c0 + c] = s;
+    }
   }
-  // transposed, split writes of the shifted values: feature c, cells r0..r0+63
-  for (int cc = ty; cc < ZT; cc += 4) {
-    const float z = valid[tx] ? t[tx][cc] - dl[cc] : 0.f;
-    const __nv_bfloat16 h = __float2bfloat16_rn(z);
-    const __nv_bfloat16 l = __float2bfloat16_rn(z - __bfloat162float(h));
-    const int64_t o = int64_t(c0 + cc) * n_pad + r0 + tx;
-    hi[o] = h;
-    lo[o] = l;
+  // transposed split writes: feature cc, cells 2p and 2p+1 of the tile
+  for (int task = tid; task < ZT * (ZR / 2); task += 256) {
+    const int cc = task >> 6, p = task & 63;
+    const int rr = 2 * p;
+    if (r0 + rr >= n_pad) continue;
+    __nv_bfloat16 h2[2], l2[2];
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const float z = valid[rr + e] ? t[rr + e][cc] - dl[cc] : 0.f;
+      h2[e] = __float2bfloat16_rn(z);
+      l2[e] = __float2bfloat16_rn(z - __bfloat162float(h2[e]));
+    }
+    const int64_t o = int64_t(c0 + cc) * n_pad + r0 + rr;
+    *reinterpret_cast<__nv_bfloat162*>(hi + o) = __halves2bfloat162(h2[0], h2[1]);
+    *reinterpret_cast<__nv_bfloat162*>(lo + o) = __halves2bfloat162(l2[0], l2[1]);
   }
 }
 
@@ -281,12 +323,28 @@ cov_tc_reduce_kernel(const float* __restrict__ part, int nsplit, int ntile, int 
   if (i != j) cov[int64_t(i) * n_cols + j] += s;
 }
 
-__global__ void zpart_reduce_kernel(const float* __restrict__ zpart, int ntiles, int h_pad, int n_cols,
+// Column sums of z from the 64-row tile partials, in FP64 and a fixed order:
+// groups of kZGroup tiles (more for very tall inputs, so that the groups fit
+// one grid dimension) in parallel, tiles in order within a group, then the
+// groups in order.
+constexpr int kZGroup = 128;
+
+__global__ void zpart_group_kernel(const float* __restrict__ zpart, int ntiles, int group, int h_pad, int n_cols,
+                                   double* __restrict__ gsum) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_cols) return;
+  const int t0 = blockIdx.y * group, t1 = min(ntiles, t0 + group);
+  double s = 0.0;
+  for (int t = t0; t < t1; ++t) s += double(zpart[int64_t(t) * h_pad + j]);
+  gsum[int64_t(blockIdx.y) * n_cols + j] = s;
+}
+
+__global__ void zpart_reduce_kernel(const double* __restrict__ gsum, int ngroups, int n_cols,
                                     double* __restrict__ zsum, double* __restrict__ zcall) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n_cols) return;
   double s = 0.0;
-  for (int t = 0; t < ntiles; ++t) s += double(zpart[int64_t(t) * h_pad + j]);
+  for (int g = 0; g < ngroups; ++g) s += gsum[int64_t(g) * n_cols + j];
   zsum[j] += s;
   zcall[j] = s;
 }
@@ -330,9 +388,11 @@ int sg_covariance_tc(sg_handle* h, const float* x, int64_t n_rows, int32_t n_col
   int64_t sps = std::max<int64_t>(8, sg::ceil_div(total_steps, want));
   const int nsplit = int(sg::ceil_div(total_steps, sps));
   const int zt = int(n_pad / ZT);
+  const int zgroup = std::max(kZGroup, sg::ceil_div_i(zt, 65535));
   const size_t need = 2 * sg::Carver::need(size_t(h_pad) * n_pad * 2) +
                       sg::Carver::need(size_t(nsplit) * ntile * TILE_ELEMS * 2 * sizeof(float)) +
                       sg::Carver::need(size_t(zt) * h_pad * 4) + sg::Carver::need(size_t(n_cols) * 8) +
+                      sg::Carver::need(size_t(sg::ceil_div_i(zt, zgroup)) * n_cols * 8) +
                       sg::Carver::need(sizeof(unsigned long long)) +
                       sg::Carver::need(sizeof(int));
   int status;
@@ -344,6 +404,8 @@ int sg_covariance_tc(sg_handle* h, const float* x, int64_t n_rows, int32_t n_col
   float* part = cv.take<float>(size_t(nsplit) * ntile * TILE_ELEMS * 2);
   float* zpart = cv.take<float>(size_t(zt) * h_pad);
   double* zcall = cv.take<double>(size_t(n_cols));
+  const int zgroups = sg::ceil_div_i(zt, zgroup);
+  double* gsum = cv.take<double>(size_t(zgroups) * n_cols);
   unsigned long long* count = cv.take<unsigned long long>(1);
   int* err = cv.take<int>(1);
   SG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
@@ -355,8 +417,13 @@ int sg_covariance_tc(sg_handle* h, const float* x, int64_t n_rows, int32_t n_col
   }
   {
     sg::ProfScope prof(h, "zsplit", st);
-    zsplit_kernel<<<dim3(unsigned(zt), unsigned(h_pad / ZT)), 256, 0, st>>>(x, n_rows, n_cols, ld, mu32, sigma32,
-                                                                          row_mask, zh, zl, n_pad, zpart, h_pad);
+    const dim3 zgrid(unsigned(sg::ceil_div(n_pad, ZR)), unsigned(h_pad / ZT));
+    if (ld % 4 == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0)
+      zsplit_kernel<true><<<zgrid, 256, 0, st>>>(x, n_rows, n_cols, ld, mu32, sigma32, row_mask, zh, zl, n_pad, zpart,
+                                                  h_pad);
+    else
+      zsplit_kernel<false><<<zgrid, 256, 0, st>>>(x, n_rows, n_cols, ld, mu32, sigma32, row_mask, zh, zl, n_pad, zpart,
+                                                   h_pad);
     SG_LAUNCH_CHECK();
   }
   CUtensorMap mAh, mAl, mBh, mBl;
@@ -379,7 +446,10 @@ int sg_covariance_tc(sg_handle* h, const float* x, int64_t n_rows, int32_t n_col
   cov_tc_reduce_kernel<<<dim3(unsigned(TILE_ELEMS / 256), unsigned(ntile)), 256, 0, st>>>(part, nsplit, ntile, TI, TJ,
                                                                                          n_cols, cov);
   SG_LAUNCH_CHECK();
-  zpart_reduce_kernel<<<sg::ceil_div_i(n_cols, 256), 256, 0, st>>>(zpart, zt, h_pad, n_cols, zsum, zcall);
+  zpart_group_kernel<<<dim3(unsigned(sg::ceil_div_i(n_cols, 256)), unsigned(zgroups)), 256, 0, st>>>(
+      zpart, zt, zgroup, h_pad, n_cols, gsum);
+  SG_LAUNCH_CHECK();
+  zpart_reduce_kernel<<<sg::ceil_div_i(n_cols, 256), 256, 0, st>>>(gsum, zgroups, n_cols, zsum, zcall);
   SG_LAUNCH_CHECK();
   cov_shift_kernel<<<dim3(unsigned(sg::ceil_div_i(n_cols, 256)), unsigned(n_cols)), 256, 0, st>>>(
       mu32, sigma32, zcall, row_mask ? count : nullptr, n_rows, n_cols, cov);

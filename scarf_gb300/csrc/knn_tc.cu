@@ -378,45 +378,81 @@ knn_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ C
 //   norms[] = |r_b|^2 (+inf for padding).
 // queries: -2 * rounded rows (exact in BF16) and, with `fold`, ones in columns
 //   d..d+2. The accumulator is then |r|^2 - 2 q.r directly.
-__global__ void refs_bf16_kernel(const float* __restrict__ in, int64_t n, int d, int ld, int fold,
-                                 __nv_bfloat16* __restrict__ out, int64_t n_pad, float* __restrict__ norms,
-                                 const int* __restrict__ perm) {
-  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (r >= n_pad) return;
-  float s = 0.f;
-  __nv_bfloat16* o = out + r * BK;
-  const int64_t src = (perm != nullptr && r < n) ? int64_t(perm[r]) : r;
-  for (int c = 0; c < d; ++c) {
-    const __nv_bfloat16 b = __float2bfloat16_rn(r < n ? in[src * ld + c] : 0.f);
-    o[c] = b;
-    const float bf = __bfloat162float(b);
-    s = fmaf(bf, bf, s);
-  }
-  for (int c = d; c < BK; ++c) o[c] = __float2bfloat16_rn(0.f);
-  if (fold && r >= n) o[d] = __float2bfloat16_rn(1e38f);  // padding: a key no query keeps
-  if (fold && r < n) {
-    const __nv_bfloat16 hi = __float2bfloat16_rn(s);
-    const float rem1 = s - __bfloat162float(hi);
-    const __nv_bfloat16 mid = __float2bfloat16_rn(rem1);
-    const __nv_bfloat16 lo = __float2bfloat16_rn(rem1 - __bfloat162float(mid));
-    o[d] = hi;
-    o[d + 1] = mid;
-    o[d + 2] = lo;
-  }
-  norms[r] = r < n ? s : __int_as_float(0x7f800000);
-}
+// Both operands are packed 64 rows per CTA: the rows (gathered through perm
+// when given) are staged in shared memory with coalesced loads, each row's
+// norm is summed by one thread in column order, and the BF16 rows leave in
+// 16-byte stores. kRef: the references as described above, and their FP32
+// norms (+inf for padding rows); otherwise the queries.
+constexpr int PR = 64;  // rows per packing CTA
 
-__global__ void queries_bf16_kernel(const float* __restrict__ in, int64_t n, int d, int ld, int fold,
-                                    __nv_bfloat16* __restrict__ out, int64_t n_pad, const int* __restrict__ perm) {
-  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (r >= n_pad) return;
-  __nv_bfloat16* o = out + r * BK;
-  const int64_t src = (perm != nullptr && r < n) ? int64_t(perm[r]) : r;
-  for (int c = 0; c < d; ++c) {
-    const float v = __bfloat162float(__float2bfloat16_rn(r < n ? in[src * ld + c] : 0.f));
-    o[c] = __float2bfloat16_rn(-2.f * v);
+template <bool kRef>
+__global__ void __launch_bounds__(256)
+pack_bf16_kernel(const float* __restrict__ in, int64_t n, int d, int ld, int fold, __nv_bfloat16* __restrict__ out,
+                 int64_t n_pad, float* __restrict__ norms, const int* __restrict__ perm) {
+  __shared__ float rows[PR][BK + 1];
+  __shared__ float nrm[PR];
+  const int64_t r0 = int64_t(blockIdx.x) * PR;
+  const int tid = threadIdx.x;
+  for (int task = tid; task < PR * BK; task += 256) {
+    const int rr = task >> 6, c = task & (BK - 1);
+    const int64_t r = r0 + rr;
+    float v = 0.f;
+    if (r < n && c < d) {
+      const int64_t src = perm != nullptr ? int64_t(perm[r]) : r;
+      v = in[src * ld + c];
+    }
+    rows[rr][c] = v;
   }
-  for (int c = d; c < BK; ++c) o[c] = __float2bfloat16_rn((fold && c < d + 3) ? 1.f : 0.f);
+  __syncthreads();
+  if (kRef && tid < PR) {
+    const int64_t r = r0 + tid;
+    float sum = 0.f;
+    for (int c = 0; c < d; ++c) {
+      const float bf = __bfloat162float(__float2bfloat16_rn(rows[tid][c]));
+      sum = fmaf(bf, bf, sum);
+    }
+    nrm[tid] = sum;
+    if (r < n_pad) norms[r] = r < n ? sum : __int_as_float(0x7f800000);
+  }
+  __syncthreads();
+  for (int task = tid; task < PR * (BK / 8); task += 256) {
+    const int rr = task >> 3, c0 = (task & 7) * 8;
+    const int64_t r = r0 + rr;
+    if (r >= n_pad) continue;
+    const bool real = r < n;
+    __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int c = c0 + e;
+      __nv_bfloat16 b;
+      if (kRef) {
+        b = __float2bfloat16_rn(0.f);
+        if (c < d) {
+          b = __float2bfloat16_rn(rows[rr][c]);
+        } else if (fold && c < d + 3) {
+          if (!real) {
+            if (c == d) b = __float2bfloat16_rn(1e38f);  // padding: a key no query keeps
+          } else {
+            const float sum = nrm[rr];
+            const __nv_bfloat16 hi = __float2bfloat16_rn(sum);
+            const float rem1 = sum - __bfloat162float(hi);
+            const __nv_bfloat16 mid = __float2bfloat16_rn(rem1);
+            const __nv_bfloat16 lo = __float2bfloat16_rn(rem1 - __bfloat162float(mid));
+            b = c == d ? hi : (c == d + 1 ? mid : lo);
+          }
+        }
+      } else {
+        if (c < d) {
+          const float v = __bfloat162float(__float2bfloat16_rn(rows[rr][c]));
+          b = __float2bfloat16_rn(-2.f * v);
+        } else {
+          b = __float2bfloat16_rn((fold && c < d + 3) ? 1.f : 0.f);
+        }
+      }
+      o[e] = b;
+    }
+    *reinterpret_cast<uint4*>(out + r * BK + c0) = *reinterpret_cast<const uint4*>(o);
+  }
 }
 
 // ---- locality order of a self-kNN ---------------------------------------
@@ -631,9 +667,10 @@ int sg_knn_tc(sg_handle* h, const float* queries, int64_t nq, const float* refs,
   SG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
   // all ones: decodes to NaN, which fminf ignores (no bound yet)
   SG_CUDA(cudaMemsetAsync(qbound, 0xFF, sizeof(unsigned) * size_t(nq_pad), st));
-  refs_bf16_kernel<<<sg::ceil_div_i(nr_pad, 256), 256, 0, st>>>(refs, nr, d, ld, fold, Rb, nr_pad, rn, perm);
+  pack_bf16_kernel<true><<<sg::ceil_div_i(nr_pad, PR), 256, 0, st>>>(refs, nr, d, ld, fold, Rb, nr_pad, rn, perm);
   SG_LAUNCH_CHECK();
-  queries_bf16_kernel<<<sg::ceil_div_i(nq_pad, 256), 256, 0, st>>>(queries, nq, d, ld, fold, Qb, nq_pad, perm);
+  pack_bf16_kernel<false><<<sg::ceil_div_i(nq_pad, PR), 256, 0, st>>>(queries, nq, d, ld, fold, Qb, nq_pad, nullptr,
+                                                                       perm);
   SG_LAUNCH_CHECK();
   CUtensorMap ta, tb;
   int rc = make_map(&ta, Qb, nq_pad, BQ);

@@ -272,3 +272,32 @@ def test_projection_narrow_features_and_widest_basis(gpu, h, dims):
         torch.cuda.synchronize()
         got = s[:, :dims].cpu().numpy()
         assert np.abs(got - want).max() <= tol * max(1.0, np.abs(want).max()), form
+
+
+@pytest.mark.parametrize("h", [300, 257])
+def test_covariance_precision_unaligned_rows_equal_aligned(gpu, h):
+    """The 3xBF16 scatter reads its rows as 16-byte vectors when every row
+    starts on a 16-byte boundary and element by element otherwise (an odd row
+    stride, or a matrix starting one float in): both give the same bits, also
+    with a row mask and a ragged last tile."""
+    from scarf_gb300 import kernels as K
+    g = torch.Generator(device="cuda").manual_seed(h)
+    n = 5_000 + 37
+    base = torch.rand((n, h), generator=g, device="cuda") * torch.rand(h, generator=g, device="cuda")
+    base[base < 0.6] = 0.0
+    aligned = torch.zeros((n, K.round_up(h, 4)), device="cuda")
+    aligned[:, :h] = base
+    odd = torch.zeros((n, h + 1), device="cuda")          # row stride h + 1: rows not 16-byte aligned
+    odd[:, :h] = base
+    shifted = torch.zeros(n * (h + 4) + 1, device="cuda")[1:].view(n, h + 4)   # starts one float in
+    shifted[:, :h] = base
+    mu = base.double().mean(0).float()
+    sg = base.double().std(0).float()
+    sg = torch.where(sg > 0, sg, torch.ones_like(sg))    # all-zero columns: sigma 1, as clean_array sets it
+    mask = torch.from_numpy((np.arange(n) % 5 != 2).astype(np.uint8)).cuda()
+    for rm in (None, mask):
+        want = K.covariance(aligned, mu, sg, n_cols=h, row_mask=rm, precision="precision")
+        for x in (odd, shifted):
+            got = K.covariance(x, mu, sg, n_cols=h, row_mask=rm, precision="precision")
+            torch.cuda.synchronize()
+            assert torch.equal(got[0], want[0]) and torch.equal(got[1], want[1])
