@@ -113,9 +113,15 @@ class RNAassay:
         self._pinned = None
         if torch.device(device).type == "cuda" and torch.cuda.is_available() and len(ind):
             # page-locked copies, which the normalisation kernel reads over the
-            # host link itself (no staging copy of the counts on the device)
-            self._pinned = [torch.from_numpy(a).pin_memory() for a in (ip, ind, dat)]
-            ip, ind, dat = (t.numpy() for t in self._pinned)
+            # host link itself (no staging copy of the counts on the device);
+            # when the host cannot lock that much memory the counts stay
+            # pageable and are copied to the device instead
+            try:
+                self._pinned = [torch.from_numpy(a).pin_memory() for a in (ip, ind, dat)]
+                ip, ind, dat = (t.numpy() for t in self._pinned)
+            except RuntimeError as e:
+                log.warning(f"counts stay in pageable memory ({e}); they are copied to the device per use")
+                self._pinned = None
         self.indptr, self.indices, self.data = ip, ind, dat
         self.n_genes = int(n_genes)
         self.cells = cells
