@@ -158,6 +158,8 @@ def peaks():
 # commands and per-kernel tables are kept under profiles/). At C2 "normalize"
 # is the row pass, the column-statistics pass and the partial reductions
 # together, and "smooth" the smoothing kernel with its two chunk kernels.
+# Only the line's dominant kernel (knn_tc) feeds roofline.traffic; the zsplit
+# and rerank figures were captured before their 16-byte-load forms.
 DRAM_TRAFFIC = {
     "c2:normalize": 3_442_579_776, "c2:zsplit": 1_596_928_704, "c2:cov_tc": 1_729_305_792,
     "c2:project": 831_836_245, "c2:knn_tc": 25_911_808, "c2:rerank": 36_871_680, "c2:smooth": 36_306_773,
