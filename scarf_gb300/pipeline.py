@@ -236,7 +236,7 @@ def make_graph(indptr, indices, data, n_genes: int, feat_idx, dims: int = 11, k:
 
 def make_graphs(samples, n_genes: int, feat_idx, dims: int = 30, k: int = 15, *, precision: str = "precision",
                 union: bool = True, n_streams: int = 16, device="cuda", **kw) -> list:
-    """Graphs of many independent samples (config C5: hundreds of samples of
+    """Graphs of many independent samples (for instance hundreds of samples of
     500-20,000 cells). ``samples`` is a sequence of ``(indptr, indices, data)``
     CSR triples sharing the gene space and the feature list. Each sample runs
     ``make_graph`` (and, with ``union``, the fuzzy union of its graph) on one
