@@ -12,6 +12,7 @@ Step order and parameters follow DataStore.make_graph
 """
 from __future__ import annotations
 
+import threading
 from dataclasses import dataclass, field
 from typing import Optional
 
@@ -57,6 +58,20 @@ class GraphResult:
 
     def recall(self) -> float:
         return 100.0 * (self.n_cells - int(self.n_missed.item())) / self.n_cells
+
+
+# page-locked host arrays that a queued kernel reads in place, each held until
+# the event recorded after its launch has completed (a later call drops them)
+_inflight = []
+_inflight_lock = threading.Lock()
+
+
+def _hold_until_done(tensors, dev):
+    ev = torch.cuda.Event()
+    ev.record(torch.cuda.current_stream(dev))
+    with _inflight_lock:
+        _inflight[:] = [(e, t) for e, t in _inflight if not e.query()]
+        _inflight.append((ev, tuple(tensors)))
 
 
 def _to_device(a, dtype, dev, stream=None):
@@ -124,6 +139,7 @@ def normalize_csr_host(indptr, indices, data, n_genes: int, feat_idx, *, size_fa
                             log_transform=log_transform, renormalize_subset=renormalize_subset,
                             n_counts=None if nc is None else nc[a:b], missing_mask=mm, fill_value=fill_value,
                             out=x[a:b], colsum=cs, colsumsq=cq, device=dev)
+        _hold_until_done((ip_h, ind_h, dat_h), dev)
         return x, cs, cq
     if not chunk_cells or chunk_cells >= n:
         ip = ip_h.to(dev, non_blocking=True)
@@ -247,7 +263,6 @@ def make_graphs(samples, n_genes: int, feat_idx, dims: int = 30, k: int = 15, *,
     import concurrent.futures as cf
     dev = torch.device(device)
     out = [None] * len(samples)
-    import threading
     streams = [torch.cuda.Stream(dev) for _ in range(max(1, n_streams))]
     local = {}
     lock = threading.Lock()
