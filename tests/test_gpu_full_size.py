@@ -8,8 +8,9 @@ graph_datastore.py:513-1020).
 
 * a1/a3: normalised rows finite and non-negative; mu and sigma against FP64
   sums of sampled columns of the normalised matrix;
-* a4: at 100,000 cells the leading principal axes against an FP64
-  eigendecomposition of the FP64 scatter (the oracle's exact PCA);
+* a4: at 100,000 cells the well separated leading axes and the span of the
+  first 10 against an FP64 eigendecomposition of the FP64 scatter (the
+  oracle's exact PCA);
 * a6/a7: distances ascending along each row, no self, indices in range,
   (nearly) every cell's first hit itself; tie-aware recall@k >= 0.995 on 500 sampled
   rows against exact FP64 kNN of the graph's own scores;
@@ -84,7 +85,7 @@ def c100k():
 
 
 def test_100k_cells_make_graph_properties(c100k):
-    from scarf_gb300 import kernels as K
+    from scarf_gb300 import kernels
     from scarf_gb300 import pipeline
     csr, feat = c100k
     n = csr.n_cells
@@ -99,10 +100,13 @@ def test_100k_cells_make_graph_properties(c100k):
     del z
     rel = (evals[:-1] - evals[1:]) / evals[0]
     m = max([i + 1 for i, r in enumerate(rel) if r > 0.02] or [1])
-    ang = oracle.subspace_angles(res.loadings[:, :m].cpu().numpy(), want[:, :m]).max()
-    assert m >= 3 and ang < 1e-4, f"principal angle {ang} over the first {m} axes"
+    got = res.loadings.cpu().numpy()
+    ang = oracle.subspace_angles(got[:, :m], want[:, :m]).max()
+    assert ang < 1e-4, f"principal angle {ang} over the first {m} axes"
+    ang10 = oracle.subspace_angles(got[:, :10], want[:, :10]).max()
+    assert ang10 < 1e-4, f"principal angle {ang10} over the first 10 axes"
     # a9: the fuzzy union is symmetric, values in (0, 1]
-    ip, ind, val = K.fuzzy_union(res.edges, res.weights, n, res.k)
+    ip, ind, val = kernels.fuzzy_union(res.edges, res.weights, n, res.k)
     u = sp.csr_matrix((val.cpu().numpy(), ind.cpu().numpy(), ip.cpu().numpy()), shape=(n, n))
     assert (u != u.T).nnz == 0
     assert u.data.min() > 0.0 and u.data.max() <= 1.0
